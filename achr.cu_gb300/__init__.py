@@ -1,0 +1,316 @@
+"""GB300-native ACHR sampler: Python mirror of the reference's ACHRCuda flow.
+
+The product is the C-ABI library ``_build/libachr_gb300.so`` (CUDA kernels for
+sm_103a plus host set-up and I/O) and the ``ACHRCuda`` command line built
+beside it.  This module binds that ABI with ctypes for tests, benchmarks and
+Python users; it performs no sampling work itself and has no CPU fallback.
+
+The directory name contains a dot, so it is loaded by file path and
+registered as the module ``achr_gb300`` (see ``load_package`` in
+``__graft_entry__``).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+import os
+from dataclasses import dataclass
+from pathlib import Path
+from typing import Optional
+
+import numpy as np
+
+PKG_DIR = Path(__file__).resolve().parent
+INCLUDE_HEADER = PKG_DIR.parent / "include" / "achr.h"
+
+MODE_REFERENCE = 0
+MODE_FEASIBLE = 1
+NULL_SVD_STS = 0
+NULL_SVD_S = 1
+
+STATUS_NAMES = {
+    0: "ACHR_OK", 1: "ACHR_ERR_INVALID", 2: "ACHR_ERR_CUDA", 3: "ACHR_ERR_NOMEM", 4: "ACHR_ERR_IO",
+    5: "ACHR_ERR_PARSE", 6: "ACHR_ERR_NUMERIC", 7: "ACHR_ERR_TIMEOUT", 8: "ACHR_ERR_UNSUPPORTED",
+}
+
+
+class AchrError(RuntimeError):
+    """A call through the C ABI returned a non-zero achr_status."""
+
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {message}")
+        self.status = status
+
+
+class Model(C.Structure):
+    _fields_ = [
+        ("n_rxns", C.c_int32), ("n_mets", C.c_int32), ("nnz", C.c_int64),
+        ("row", C.POINTER(C.c_int32)), ("col", C.POINTER(C.c_int32)), ("val", C.POINTER(C.c_double)),
+        ("lb", C.POINTER(C.c_double)), ("ub", C.POINTER(C.c_double)),
+    ]
+
+
+class ModelBuf(C.Structure):
+    _fields_ = [
+        ("model", Model),
+        ("row_buf", C.POINTER(C.c_int32)), ("col_buf", C.POINTER(C.c_int32)),
+        ("val_buf", C.POINTER(C.c_double)), ("lb_buf", C.POINTER(C.c_double)), ("ub_buf", C.POINTER(C.c_double)),
+    ]
+
+
+class Options(C.Structure):
+    _fields_ = [
+        ("mode", C.c_int32), ("null_space", C.c_int32), ("check_period", C.c_int32), ("max_attempts", C.c_int32),
+        ("centre_offset", C.c_int32), ("exact_ratio", C.c_int32), ("threads_per_chain", C.c_int32),
+        ("reserved", C.c_int32),
+        ("residual_tol", C.c_double), ("max_min_tol", C.c_double), ("u_tol", C.c_double), ("d_tol", C.c_double),
+        ("feasibility_tol", C.c_double),
+    ]
+
+
+class Stats(C.Structure):
+    _fields_ = [
+        ("accepted", C.c_int64), ("rejected", C.c_int64), ("checks", C.c_int64), ("reprojections", C.c_int64),
+        ("stuck_chains", C.c_int64), ("exact_evals", C.c_int64), ("final_projections", C.c_int64),
+        ("max_residual", C.c_double), ("max_bound_violation", C.c_double), ("kernel_ms", C.c_double),
+    ]
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+# Every symbol include/achr.h declares, with its ctypes signature.
+_SIGNATURES = {
+    "achr_default_options": (None, [C.POINTER(Options)]),
+    "achr_create": (C.c_int, [C.POINTER(Model), C.POINTER(C.c_double), C.c_int32, C.POINTER(Options),
+                              C.POINTER(C.c_void_p)]),
+    "achr_set_null_space": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.c_int32]),
+    "achr_get_null_space_dim": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
+    "achr_get_null_space": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
+    "achr_get_centre": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
+    "achr_sample": (C.c_int, [C.c_void_p, C.c_uint64, C.c_uint64, C.c_int32, C.c_int32, C.POINTER(C.c_double),
+                              C.POINTER(Stats)]),
+    "achr_sample_device": (C.c_int, [C.c_void_p, C.c_uint64, C.c_uint64, C.c_int32, C.c_int32, C.c_void_p,
+                                     C.c_int64, C.c_void_p, C.POINTER(Stats)]),
+    "achr_destroy": (None, [C.c_void_p]),
+    "achr_read_mps": (C.c_int, [C.c_char_p, C.POINTER(ModelBuf)]),
+    "achr_free_model": (None, [C.POINTER(ModelBuf)]),
+    "achr_read_warmup_csv": (C.c_int, [C.c_char_p, C.c_int32, C.POINTER(C.POINTER(C.c_double)),
+                                       C.POINTER(C.c_int32)]),
+    "achr_write_points_csv": (C.c_int, [C.c_char_p, C.POINTER(C.c_double), C.c_int32, C.c_int32, C.c_int32]),
+    "achr_format_f": (C.c_int32, [C.c_double, C.c_char_p]),
+    "achr_free": (None, [C.c_void_p]),
+    "achr_last_error": (C.c_char_p, []),
+    "achr_version": (C.c_int32, []),
+}
+
+_lib: Optional[C.CDLL] = None
+
+
+def library_path() -> Path:
+    return PKG_DIR / "_build" / "libachr_gb300.so"
+
+
+def cli_path() -> Path:
+    return PKG_DIR / "_build" / "ACHRCuda"
+
+
+def lib() -> C.CDLL:
+    """Load the native library; raises if it has not been built (no fallback)."""
+    global _lib
+    if _lib is None:
+        path = library_path()
+        if not path.exists():
+            raise ImportError(f"native library {path} is missing: run __graft_entry__.build() first")
+        handle = C.CDLL(str(path))
+        for name, (res, args) in _SIGNATURES.items():
+            fn = getattr(handle, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = handle
+    return _lib
+
+
+def _check(status: int) -> None:
+    if status != 0:
+        msg = lib().achr_last_error()
+        raise AchrError(status, msg.decode() if msg else "")
+
+
+def _dptr(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _iptr(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_int32))
+
+
+def default_options(**overrides) -> Options:
+    opt = Options()
+    lib().achr_default_options(C.byref(opt))
+    for k, v in overrides.items():
+        if not hasattr(opt, k):
+            raise KeyError(k)
+        setattr(opt, k, v)
+    return opt
+
+
+@dataclass
+class HostModel:
+    """S as COO triplets plus bounds, the part of an MPS model the sampler uses."""
+    n_rxns: int
+    n_mets: int
+    row: np.ndarray
+    col: np.ndarray
+    val: np.ndarray
+    lb: np.ndarray
+    ub: np.ndarray
+
+    def dense(self) -> np.ndarray:
+        S = np.zeros((self.n_mets, self.n_rxns))
+        np.add.at(S, (self.row, self.col), self.val)
+        return S
+
+    def _as_struct(self):
+        keep = (np.ascontiguousarray(self.row, dtype=np.int32), np.ascontiguousarray(self.col, dtype=np.int32),
+                np.ascontiguousarray(self.val, dtype=np.float64), np.ascontiguousarray(self.lb, dtype=np.float64),
+                np.ascontiguousarray(self.ub, dtype=np.float64))
+        m = Model(self.n_rxns, self.n_mets, len(keep[0]), _iptr(keep[0]), _iptr(keep[1]), _dptr(keep[2]),
+                  _dptr(keep[3]), _dptr(keep[4]))
+        return m, keep
+
+
+def read_mps(path: str | os.PathLike) -> HostModel:
+    """Read a fixed-format MPS file through the library's reader."""
+    mb = ModelBuf()
+    _check(lib().achr_read_mps(str(path).encode(), C.byref(mb)))
+    try:
+        m = mb.model
+        nnz = m.nnz
+        hm = HostModel(m.n_rxns, m.n_mets,
+                       np.ctypeslib.as_array(m.row, (nnz,)).copy() if nnz else np.zeros(0, np.int32),
+                       np.ctypeslib.as_array(m.col, (nnz,)).copy() if nnz else np.zeros(0, np.int32),
+                       np.ctypeslib.as_array(m.val, (nnz,)).copy() if nnz else np.zeros(0),
+                       np.ctypeslib.as_array(m.lb, (m.n_rxns,)).copy(),
+                       np.ctypeslib.as_array(m.ub, (m.n_rxns,)).copy())
+    finally:
+        lib().achr_free_model(C.byref(mb))
+    return hm
+
+
+def read_warmup_csv(path: str | os.PathLike, n_rxns: int) -> np.ndarray:
+    """Read a warmup CSV into an (n, W) array (column j = warmup point j)."""
+    ptr = C.POINTER(C.c_double)()
+    W = C.c_int32()
+    _check(lib().achr_read_warmup_csv(str(path).encode(), n_rxns, C.byref(ptr), C.byref(W)))
+    try:
+        flat = np.ctypeslib.as_array(ptr, (W.value * n_rxns,)).copy()
+    finally:
+        lib().achr_free(ptr)
+    return flat.reshape(W.value, n_rxns).T.copy()
+
+
+def write_points_csv(path: str | os.PathLike, points: np.ndarray, threads: int = 0) -> None:
+    """Write an (n, P) array as the reference's File<ii>."""
+    pts = np.ascontiguousarray(points, dtype=np.float64)
+    n, P = pts.shape
+    _check(lib().achr_write_points_csv(str(path).encode(), _dptr(pts), n, P, threads))
+
+
+def format_f(v: float) -> str:
+    buf = C.create_string_buffer(400)
+    k = lib().achr_format_f(float(v), buf)
+    return buf.raw[:k].decode()
+
+
+class Sampler:
+    """One model and its warmup points resident on the GPU.
+
+    Mirrors the reference program's flow (ACHRcu/ACHRCuda.cu:504-802): set-up
+    (null space, centre) once, then one ``sample`` call per output file.
+    """
+
+    def __init__(self, model: HostModel, warmup: np.ndarray, options: Optional[Options] = None, **overrides):
+        self.model = model
+        self.n = model.n_rxns
+        w = np.asarray(warmup, dtype=np.float64)
+        if w.ndim != 2 or w.shape[0] != self.n:
+            raise ValueError("warmup must be an (n_rxns, W) array")
+        self.W = w.shape[1]
+        wcol = np.asfortranarray(w)  # column j contiguous
+        opt = options if options is not None else default_options(**overrides)
+        self.options = opt
+        m, keep = model._as_struct()
+        ctx = C.c_void_p()
+        _check(lib().achr_create(C.byref(m), wcol.ctypes.data_as(C.POINTER(C.c_double)), self.W, C.byref(opt),
+                                 C.byref(ctx)))
+        del keep
+        self._ctx = ctx
+
+    def close(self) -> None:
+        if getattr(self, "_ctx", None):
+            lib().achr_destroy(self._ctx)
+            self._ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @property
+    def null_dim(self) -> int:
+        d = C.c_int32()
+        _check(lib().achr_get_null_space_dim(self._ctx, C.byref(d)))
+        return d.value
+
+    def null_space(self) -> np.ndarray:
+        d = self.null_dim
+        out = np.zeros(self.n * d)
+        if d:
+            _check(lib().achr_get_null_space(self._ctx, _dptr(out)))
+        return out.reshape(d, self.n).T.copy()
+
+    def set_null_space(self, N: np.ndarray) -> None:
+        Nf = np.asfortranarray(np.asarray(N, dtype=np.float64))
+        if Nf.shape[0] != self.n:
+            raise ValueError("N must have n_rxns rows")
+        _check(lib().achr_set_null_space(self._ctx, Nf.ctypes.data_as(C.POINTER(C.c_double)), Nf.shape[1]))
+
+    def centre(self) -> np.ndarray:
+        out = np.zeros(self.n)
+        _check(lib().achr_get_centre(self._ctx, _dptr(out)))
+        return out
+
+    def sample(self, n_points: int, n_steps: int, seed: int = 0, chain_offset: int = 0,
+               out: Optional[np.ndarray] = None) -> tuple[np.ndarray, dict]:
+        """Run n_points chains of n_steps; returns ((n, P) points, stats)."""
+        if out is None:
+            out = np.empty((self.n, n_points))
+        if out.shape != (self.n, n_points) or out.dtype != np.float64 or not out.flags.c_contiguous:
+            raise ValueError("out must be a C-contiguous float64 (n_rxns, n_points) array")
+        st = Stats()
+        _check(lib().achr_sample(self._ctx, seed, chain_offset, n_points, n_steps, _dptr(out), C.byref(st)))
+        return out, st.as_dict()
+
+    def sample_device(self, n_points: int, n_steps: int, d_out: int, ld_out: int, stream: int = 0, seed: int = 0,
+                      chain_offset: int = 0, with_stats: bool = False) -> Optional[dict]:
+        """Queue sampling into device memory d_out (n x ld_out row-major) on a CUDA stream."""
+        st = Stats() if with_stats else None
+        _check(lib().achr_sample_device(self._ctx, seed, chain_offset, n_points, n_steps, C.c_void_p(d_out), ld_out,
+                                        C.c_void_p(stream), C.byref(st) if st is not None else None))
+        return st.as_dict() if st is not None else None
+
+
+def exported_symbols() -> list[str]:
+    """Function names declared in include/achr.h."""
+    import re
+    text = INCLUDE_HEADER.read_text()
+    names = re.findall(r"^\s*(?:const\s+)?[\w\s\*]+?\b(achr_\w+)\s*\(", text, flags=re.M)
+    return sorted(set(names))

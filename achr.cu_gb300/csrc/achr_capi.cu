@@ -1,0 +1,518 @@
+// C ABI of the sampler: context set-up (model upload, null space, centre) and
+// sampling launches.  Replaces the set-up half of the reference's main()
+// (ACHRcu/ACHRCuda.cu:642-729) and its per-file launch (:736-743).
+#include <cublas_v2.h>
+#include <cuda_runtime.h>
+#include <cusolverDn.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/achr.h"
+#include "achr_internal.h"
+
+using achr::ChainArgs;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+achr_status fail(achr_status st, const std::string &msg) {
+    g_last_error = msg;
+    return st;
+}
+
+achr_status cuda_fail(cudaError_t e, const char *what) {
+    return fail(ACHR_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define ACHR_CUDA_TRY(expr)                                     \
+    do {                                                        \
+        cudaError_t e_ = (expr);                                \
+        if (e_ != cudaSuccess) return cuda_fail(e_, #expr);     \
+    } while (0)
+
+// Device buffer that frees itself.
+template <class T>
+struct DevBuf {
+    T *p = nullptr;
+    size_t count = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf &) = delete;
+    DevBuf &operator=(const DevBuf &) = delete;
+    ~DevBuf() { reset(); }
+    void reset() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        count = 0;
+    }
+    cudaError_t alloc(size_t n) {
+        reset();
+        if (n == 0) n = 1;
+        cudaError_t e = cudaMalloc(&p, n * sizeof(T));
+        if (e == cudaSuccess) count = n;
+        else p = nullptr;
+        return e;
+    }
+    cudaError_t upload(const T *h, size_t n) {
+        cudaError_t e = alloc(n);
+        if (e != cudaSuccess) return e;
+        if (n) e = cudaMemcpy(p, h, n * sizeof(T), cudaMemcpyHostToDevice);
+        return e;
+    }
+};
+
+// Float image of a bound with a rounded-up conversion error (used by the FP32
+// ratio-test brackets of the chain kernel).
+void f32_bound(double v, float &f, float &err) {
+    if (std::isinf(v)) {
+        f = (float)v;
+        err = 0.0f;
+        return;
+    }
+    f = (float)v;
+    const double e = std::fabs(v - (double)f);
+    float ef = (float)e;
+    if ((double)ef < e) ef = std::nextafter(ef, INFINITY);
+    err = ef;
+}
+
+__global__ void centre_kernel(int n, int W, int ldw, const double *__restrict__ warmup, int centre_offset,
+                              double *__restrict__ c0, double *__restrict__ A0) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double acc = 0.0;
+    for (int j = 0; j < W; ++j) acc += warmup[(size_t)j * (size_t)ldw + i];
+    // c = (1/W) * sum_j w_j (reference createCenterPt, ACHRCuda.cu:414-434)
+    const double c = (1.0 / (double)W) * acc;
+    c0[i] = c;
+    A0[i] = (double)(W + centre_offset) * c;
+}
+
+}  // namespace
+
+struct achr_ctx {
+    int n = 0, m = 0, W = 0, d = 0, ldw = 0;
+    int device = 0;
+    achr_options opt{};
+    std::vector<double> h_lb, h_ub;
+    std::vector<int> h_rowptr, h_colidx;
+    std::vector<double> h_val;
+    DevBuf<double> warmup, c0, A0, lb, ub, val, N, points;
+    DevBuf<float4> bnd32;
+    DevBuf<int> rowptr, colidx;
+    DevBuf<unsigned long long> counters;
+};
+
+extern "C" {
+
+void achr_default_options(achr_options *opt) {
+    if (!opt) return;
+    std::memset(opt, 0, sizeof(*opt));
+    opt->mode = ACHR_MODE_REFERENCE;
+    opt->null_space = ACHR_NULL_SVD_STS;
+    opt->check_period = 10;
+    opt->max_attempts = 100000;
+    opt->centre_offset = 0;
+    opt->exact_ratio = 0;
+    opt->threads_per_chain = 0;
+    opt->residual_tol = 1e-9;
+    opt->max_min_tol = 1e-9;
+    opt->u_tol = 1e-9;
+    opt->d_tol = 1e-14;
+    opt->feasibility_tol = 1e-8;
+}
+
+const char *achr_last_error(void) { return g_last_error.c_str(); }
+
+void achr_io_set_error(const char *msg) { g_last_error = msg ? msg : ""; }
+
+int32_t achr_version(void) { return 100; }
+
+}  // extern "C"
+
+namespace {
+
+achr_status validate_options(const achr_options &o) {
+    if (o.mode != ACHR_MODE_REFERENCE && o.mode != ACHR_MODE_FEASIBLE) return fail(ACHR_ERR_INVALID, "unknown mode");
+    if (o.null_space != ACHR_NULL_SVD_STS && o.null_space != ACHR_NULL_SVD_S)
+        return fail(ACHR_ERR_INVALID, "unknown null_space method");
+    if (o.check_period <= 0) return fail(ACHR_ERR_INVALID, "check_period must be positive");
+    if (o.max_attempts <= 0) return fail(ACHR_ERR_INVALID, "max_attempts must be positive");
+    if (o.centre_offset != 0 && o.centre_offset != 1) return fail(ACHR_ERR_INVALID, "centre_offset must be 0 or 1");
+    if (o.threads_per_chain != 0 &&
+        (o.threads_per_chain < 32 || o.threads_per_chain > 512 || o.threads_per_chain % 32 != 0))
+        return fail(ACHR_ERR_INVALID, "threads_per_chain must be 0 or a multiple of 32 in [32, 512]");
+    if (!(o.residual_tol >= 0) || !(o.max_min_tol >= 0) || !(o.u_tol >= 0) || !(o.d_tol >= 0) ||
+        !(o.feasibility_tol >= 0))
+        return fail(ACHR_ERR_INVALID, "tolerances must be non-negative");
+    return ACHR_OK;
+}
+
+// Null space of S by the reference's rule: eigen-decomposition of S^T S
+// (symmetric, so its SVD and eigen-decomposition share the spectrum), cutoff
+// n * sigma_0 * 2.2204e-16; the basis is every eigenvector whose eigenvalue
+// magnitude is below the cutoff (ACHRCuda.cu:459-489).  If no value falls
+// below the cutoff the reference keeps istart = 0 and uses all n columns.
+achr_status null_space_sts(int n, int m, const std::vector<double> &denseS, std::vector<double> &N, int &d) {
+    DevBuf<double> dS, dStS, dW, work;
+    DevBuf<int> info;
+    ACHR_CUDA_TRY(dS.upload(denseS.data(), (size_t)m * n));
+    ACHR_CUDA_TRY(dStS.alloc((size_t)n * n));
+    ACHR_CUDA_TRY(dW.alloc(n));
+    ACHR_CUDA_TRY(info.alloc(1));
+    cublasHandle_t cb = nullptr;
+    if (cublasCreate(&cb) != CUBLAS_STATUS_SUCCESS) return fail(ACHR_ERR_CUDA, "cublasCreate failed");
+    const double one = 1.0, zero = 0.0;
+    cublasStatus_t bs = cublasDgemm(cb, CUBLAS_OP_T, CUBLAS_OP_N, n, n, m, &one, dS.p, m, dS.p, m, &zero, dStS.p, n);
+    cublasDestroy(cb);
+    if (bs != CUBLAS_STATUS_SUCCESS) return fail(ACHR_ERR_CUDA, "cublasDgemm (S^T S) failed");
+    cusolverDnHandle_t sh = nullptr;
+    if (cusolverDnCreate(&sh) != CUSOLVER_STATUS_SUCCESS) return fail(ACHR_ERR_CUDA, "cusolverDnCreate failed");
+    int lwork = 0;
+    cusolverStatus_t ss =
+        cusolverDnDsyevd_bufferSize(sh, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n, dStS.p, n, dW.p, &lwork);
+    if (ss == CUSOLVER_STATUS_SUCCESS) {
+        cudaError_t e = work.alloc((size_t)(lwork > 0 ? lwork : 1));
+        if (e != cudaSuccess) {
+            cusolverDnDestroy(sh);
+            return cuda_fail(e, "cudaMalloc(syevd work)");
+        }
+        ss = cusolverDnDsyevd(sh, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n, dStS.p, n, dW.p, work.p, lwork,
+                              info.p);
+    }
+    cusolverDnDestroy(sh);
+    if (ss != CUSOLVER_STATUS_SUCCESS) return fail(ACHR_ERR_NUMERIC, "cusolverDnDsyevd failed");
+    int h_info = 0;
+    std::vector<double> lam(n), V((size_t)n * n);
+    ACHR_CUDA_TRY(cudaMemcpy(&h_info, info.p, sizeof(int), cudaMemcpyDeviceToHost));
+    if (h_info != 0) return fail(ACHR_ERR_NUMERIC, "syevd did not converge (info=" + std::to_string(h_info) + ")");
+    ACHR_CUDA_TRY(cudaMemcpy(lam.data(), dW.p, sizeof(double) * n, cudaMemcpyDeviceToHost));
+    ACHR_CUDA_TRY(cudaMemcpy(V.data(), dStS.p, sizeof(double) * (size_t)n * n, cudaMemcpyDeviceToHost));
+    double smax = 0.0;
+    for (int i = 0; i < n; ++i) smax = std::max(smax, std::fabs(lam[i]));
+    const double tol = (double)n * smax * 2.2204e-16;
+    std::vector<int> cols;
+    for (int i = 0; i < n; ++i)
+        if (std::fabs(lam[i]) < tol) cols.push_back(i);
+    if (cols.empty())
+        for (int i = 0; i < n; ++i) cols.push_back(i);
+    d = (int)cols.size();
+    N.assign((size_t)n * d, 0.0);
+    for (int j = 0; j < d; ++j)
+        std::memcpy(N.data() + (size_t)j * n, V.data() + (size_t)cols[j] * n, sizeof(double) * n);
+    return ACHR_OK;
+}
+
+// Null space from the SVD of S^T (n x m, n >= m as cuSOLVER's gesvd needs):
+// left singular vectors beyond the numerical rank span null(S).  Cutoff
+// max(m,n) * sigma_0 * 2.2204e-16 on the singular values of S.
+achr_status null_space_svd_s(int n, int m, const std::vector<double> &denseS, std::vector<double> &N, int &d) {
+    if (n < m) return fail(ACHR_ERR_UNSUPPORTED, "ACHR_NULL_SVD_S needs n_rxns >= n_mets");
+    std::vector<double> St((size_t)n * m);
+    for (int i = 0; i < m; ++i)
+        for (int j = 0; j < n; ++j) St[(size_t)i * n + j] = denseS[(size_t)j * m + i];
+    DevBuf<double> dA, dSig, dU, dVT, work, rwork;
+    DevBuf<int> info;
+    ACHR_CUDA_TRY(dA.upload(St.data(), St.size()));
+    ACHR_CUDA_TRY(dSig.alloc(m));
+    ACHR_CUDA_TRY(dU.alloc((size_t)n * n));
+    ACHR_CUDA_TRY(dVT.alloc((size_t)m * m));
+    ACHR_CUDA_TRY(info.alloc(1));
+    ACHR_CUDA_TRY(rwork.alloc(m));
+    cusolverDnHandle_t sh = nullptr;
+    if (cusolverDnCreate(&sh) != CUSOLVER_STATUS_SUCCESS) return fail(ACHR_ERR_CUDA, "cusolverDnCreate failed");
+    int lwork = 0;
+    cusolverStatus_t ss = cusolverDnDgesvd_bufferSize(sh, n, m, &lwork);
+    if (ss == CUSOLVER_STATUS_SUCCESS) {
+        cudaError_t e = work.alloc((size_t)(lwork > 0 ? lwork : 1));
+        if (e != cudaSuccess) {
+            cusolverDnDestroy(sh);
+            return cuda_fail(e, "cudaMalloc(gesvd work)");
+        }
+        signed char jobu = 'A', jobvt = 'N';
+        ss = cusolverDnDgesvd(sh, jobu, jobvt, n, m, dA.p, n, dSig.p, dU.p, n, dVT.p, m, work.p, lwork, rwork.p,
+                              info.p);
+    }
+    cusolverDnDestroy(sh);
+    if (ss != CUSOLVER_STATUS_SUCCESS) return fail(ACHR_ERR_NUMERIC, "cusolverDnDgesvd failed");
+    int h_info = 0;
+    ACHR_CUDA_TRY(cudaMemcpy(&h_info, info.p, sizeof(int), cudaMemcpyDeviceToHost));
+    if (h_info != 0) return fail(ACHR_ERR_NUMERIC, "gesvd did not converge (info=" + std::to_string(h_info) + ")");
+    std::vector<double> sig(m), U((size_t)n * n);
+    ACHR_CUDA_TRY(cudaMemcpy(sig.data(), dSig.p, sizeof(double) * m, cudaMemcpyDeviceToHost));
+    ACHR_CUDA_TRY(cudaMemcpy(U.data(), dU.p, sizeof(double) * U.size(), cudaMemcpyDeviceToHost));
+    const double tol = (double)std::max(n, m) * (m > 0 ? sig[0] : 0.0) * 2.2204e-16;
+    int rank = 0;
+    for (int i = 0; i < m; ++i)
+        if (sig[i] >= tol && sig[i] > 0.0) ++rank;
+    d = n - rank;
+    N.assign((size_t)n * (d > 0 ? d : 0), 0.0);
+    for (int j = 0; j < d; ++j)
+        std::memcpy(N.data() + (size_t)j * n, U.data() + (size_t)(rank + j) * n, sizeof(double) * n);
+    return ACHR_OK;
+}
+
+achr_status upload_null_space(achr_ctx *ctx, const double *N, int d) {
+    ctx->d = d;
+    ACHR_CUDA_TRY(ctx->N.upload(N, (size_t)ctx->n * (size_t)(d > 0 ? d : 0)));
+    return ACHR_OK;
+}
+
+achr_status read_counters(achr_ctx *ctx, achr_stats *stats, float ms) {
+    unsigned long long c[achr::CNT_SLOTS];
+    ACHR_CUDA_TRY(cudaMemcpy(c, ctx->counters.p, sizeof(c), cudaMemcpyDeviceToHost));
+    if (c[achr::CNT_ERROR] & achr::ERR_TMA_TIMEOUT)
+        return fail(ACHR_ERR_TIMEOUT, "a warmup-column copy did not complete within its wait limit");
+    if (stats) {
+        stats->accepted = (int64_t)c[achr::CNT_ACCEPTED];
+        stats->rejected = (int64_t)c[achr::CNT_REJECTED];
+        stats->checks = (int64_t)c[achr::CNT_CHECKS];
+        stats->reprojections = (int64_t)c[achr::CNT_REPROJ];
+        stats->stuck_chains = (int64_t)c[achr::CNT_STUCK];
+        stats->exact_evals = (int64_t)c[achr::CNT_EXACT];
+        stats->final_projections = (int64_t)c[achr::CNT_FINAL_PROJ];
+        double r, v;
+        std::memcpy(&r, &c[achr::CNT_MAXRES_BITS], sizeof(double));
+        std::memcpy(&v, &c[achr::CNT_MAXVIOL_BITS], sizeof(double));
+        stats->max_residual = r;
+        stats->max_bound_violation = v;
+        stats->kernel_ms = ms;
+    }
+    return ACHR_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+achr_status achr_create(const achr_model *model, const double *warmup, int32_t n_warmup, const achr_options *opt_in,
+                        achr_ctx **out) {
+    if (!out) return fail(ACHR_ERR_INVALID, "out is NULL");
+    *out = nullptr;
+    if (!model || !warmup) return fail(ACHR_ERR_INVALID, "model or warmup is NULL");
+    achr_options opt;
+    if (opt_in) opt = *opt_in;
+    else achr_default_options(&opt);
+    achr_status st = validate_options(opt);
+    if (st != ACHR_OK) return st;
+    const int n = model->n_rxns, m = model->n_mets;
+    if (n <= 0 || m < 0) return fail(ACHR_ERR_INVALID, "model needs n_rxns > 0 and n_mets >= 0");
+    if (n > 16384) return fail(ACHR_ERR_UNSUPPORTED, "n_rxns > 16384 is not supported by the chain kernel");
+    if (n_warmup <= 0) return fail(ACHR_ERR_INVALID, "need at least one warmup point");
+    if (model->nnz < 0 || (model->nnz > 0 && (!model->row || !model->col || !model->val)))
+        return fail(ACHR_ERR_INVALID, "bad COO arrays");
+    if (!model->lb || !model->ub) return fail(ACHR_ERR_INVALID, "bounds are NULL");
+
+    achr_ctx *ctx = new (std::nothrow) achr_ctx();
+    if (!ctx) return fail(ACHR_ERR_NOMEM, "context allocation failed");
+    struct Guard {
+        achr_ctx *&c;
+        ~Guard() { delete c; }
+    };
+    achr_ctx *owned = ctx;
+    Guard guard{owned};
+
+    ctx->n = n;
+    ctx->m = m;
+    ctx->W = n_warmup;
+    ctx->opt = opt;
+    cudaGetDevice(&ctx->device);
+    ctx->h_lb.assign(model->lb, model->lb + n);
+    ctx->h_ub.assign(model->ub, model->ub + n);
+
+    // COO -> CSR, duplicates summed, explicit zeros dropped (the reference's
+    // dense-scan COO keeps only non-zeros, ACHRCuda.cu:647-655).
+    std::vector<int64_t> order((size_t)model->nnz);
+    for (int64_t k = 0; k < model->nnz; ++k) {
+        const int r = model->row[k], c = model->col[k];
+        if (r < 0 || r >= m || c < 0 || c >= n) return fail(ACHR_ERR_INVALID, "COO index out of range");
+        order[(size_t)k] = k;
+    }
+    std::sort(order.begin(), order.end(), [&](int64_t a, int64_t b) {
+        if (model->row[a] != model->row[b]) return model->row[a] < model->row[b];
+        return model->col[a] < model->col[b];
+    });
+    ctx->h_rowptr.assign((size_t)m + 1, 0);
+    for (size_t q = 0; q < order.size();) {
+        const int r = model->row[order[q]], c = model->col[order[q]];
+        double v = 0.0;
+        while (q < order.size() && model->row[order[q]] == r && model->col[order[q]] == c) v += model->val[order[q++]];
+        if (v != 0.0) {
+            ctx->h_colidx.push_back(c);
+            ctx->h_val.push_back(v);
+            ctx->h_rowptr[(size_t)r + 1]++;
+        }
+    }
+    for (int r = 0; r < m; ++r) ctx->h_rowptr[(size_t)r + 1] += ctx->h_rowptr[(size_t)r];
+
+    std::vector<float4> b32(n);
+    for (int i = 0; i < n; ++i) {
+        if (!(model->lb[i] <= model->ub[i])) return fail(ACHR_ERR_INVALID, "lb > ub or NaN bound at reaction " + std::to_string(i));
+        float lf, le, uf, ue;
+        f32_bound(model->lb[i], lf, le);
+        f32_bound(model->ub[i], uf, ue);
+        b32[i] = make_float4(lf, uf, le, ue);
+    }
+    for (int64_t k = 0; k < (int64_t)n * n_warmup; ++k)
+        if (!std::isfinite(warmup[k])) return fail(ACHR_ERR_INVALID, "warmup points must be finite");
+
+    ACHR_CUDA_TRY(ctx->lb.upload(model->lb, n));
+    ACHR_CUDA_TRY(ctx->ub.upload(model->ub, n));
+    ACHR_CUDA_TRY(ctx->bnd32.upload(b32.data(), n));
+    ACHR_CUDA_TRY(ctx->rowptr.upload(ctx->h_rowptr.data(), ctx->h_rowptr.size()));
+    ACHR_CUDA_TRY(ctx->colidx.upload(ctx->h_colidx.data(), ctx->h_colidx.size()));
+    ACHR_CUDA_TRY(ctx->val.upload(ctx->h_val.data(), ctx->h_val.size()));
+    ACHR_CUDA_TRY(ctx->counters.alloc(achr::CNT_SLOTS));
+
+    // Warmup matrix with an even leading dimension so every column starts on a
+    // 16-byte boundary (a TMA bulk-copy requirement).
+    ctx->ldw = (n + 1) & ~1;
+    ACHR_CUDA_TRY(ctx->warmup.alloc((size_t)ctx->ldw * n_warmup));
+    ACHR_CUDA_TRY(cudaMemset(ctx->warmup.p, 0, sizeof(double) * (size_t)ctx->ldw * n_warmup));
+    ACHR_CUDA_TRY(cudaMemcpy2D(ctx->warmup.p, sizeof(double) * ctx->ldw, warmup, sizeof(double) * n,
+                               sizeof(double) * n, n_warmup, cudaMemcpyHostToDevice));
+
+    // Null space (computeKernelCuda, ACHRCuda.cu:436-502).
+    std::vector<double> denseS((size_t)m * n, 0.0);
+    for (int r = 0; r < m; ++r)
+        for (int q = ctx->h_rowptr[r]; q < ctx->h_rowptr[(size_t)r + 1]; ++q)
+            denseS[(size_t)ctx->h_colidx[q] * m + r] = ctx->h_val[q];
+    std::vector<double> Nh;
+    int d = 0;
+    if (m == 0) {
+        // No constraints: the reference's rule keeps every column (identity basis).
+        d = n;
+        Nh.assign((size_t)n * n, 0.0);
+        for (int i = 0; i < n; ++i) Nh[(size_t)i * n + i] = 1.0;
+    } else {
+        st = (opt.null_space == ACHR_NULL_SVD_S) ? null_space_svd_s(n, m, denseS, Nh, d)
+                                                 : null_space_sts(n, m, denseS, Nh, d);
+        if (st != ACHR_OK) return st;
+    }
+    st = upload_null_space(ctx, Nh.data(), d);
+    if (st != ACHR_OK) return st;
+
+    // Centre of the warmup points and the centre accumulator.
+    ACHR_CUDA_TRY(ctx->c0.alloc(n));
+    ACHR_CUDA_TRY(ctx->A0.alloc(n));
+    centre_kernel<<<(n + 127) / 128, 128>>>(n, n_warmup, ctx->ldw, ctx->warmup.p, opt.centre_offset, ctx->c0.p,
+                                            ctx->A0.p);
+    ACHR_CUDA_TRY(cudaGetLastError());
+    ACHR_CUDA_TRY(cudaDeviceSynchronize());
+
+    owned = nullptr;  // release from the guard
+    *out = ctx;
+    g_last_error.clear();
+    return ACHR_OK;
+}
+
+achr_status achr_set_null_space(achr_ctx *ctx, const double *N, int32_t d) {
+    if (!ctx || (!N && d > 0) || d < 0 || d > ctx->n) return fail(ACHR_ERR_INVALID, "bad null-space arguments");
+    return upload_null_space(ctx, N, d);
+}
+
+achr_status achr_get_null_space_dim(const achr_ctx *ctx, int32_t *d) {
+    if (!ctx || !d) return fail(ACHR_ERR_INVALID, "NULL argument");
+    *d = ctx->d;
+    return ACHR_OK;
+}
+
+achr_status achr_get_null_space(const achr_ctx *ctx, double *N_out) {
+    if (!ctx || !N_out) return fail(ACHR_ERR_INVALID, "NULL argument");
+    if (ctx->d > 0)
+        ACHR_CUDA_TRY(cudaMemcpy(N_out, ctx->N.p, sizeof(double) * (size_t)ctx->n * ctx->d, cudaMemcpyDeviceToHost));
+    return ACHR_OK;
+}
+
+achr_status achr_get_centre(const achr_ctx *ctx, double *centre_out) {
+    if (!ctx || !centre_out) return fail(ACHR_ERR_INVALID, "NULL argument");
+    ACHR_CUDA_TRY(cudaMemcpy(centre_out, ctx->c0.p, sizeof(double) * ctx->n, cudaMemcpyDeviceToHost));
+    return ACHR_OK;
+}
+
+achr_status achr_sample_device(achr_ctx *ctx, uint64_t seed, uint64_t chain_offset, int32_t n_points, int32_t n_steps,
+                               double *d_points_out, int64_t ld_out, void *stream, achr_stats *stats) {
+    if (!ctx) return fail(ACHR_ERR_INVALID, "ctx is NULL");
+    if (n_points < 0 || n_steps < 0) return fail(ACHR_ERR_INVALID, "n_points and n_steps must be >= 0");
+    if (n_points > 0 && (!d_points_out || ld_out < n_points)) return fail(ACHR_ERR_INVALID, "bad output buffer");
+    if (chain_offset + (uint64_t)n_points < chain_offset) return fail(ACHR_ERR_INVALID, "chain ids overflow");
+    cudaStream_t s = (cudaStream_t)stream;
+    ChainArgs a{};
+    a.n = ctx->n;
+    a.m = ctx->m;
+    a.W = ctx->W;
+    a.d = ctx->d;
+    a.ldw = ctx->ldw;
+    a.P = n_points;
+    a.T = n_steps;
+    a.warmup = ctx->warmup.p;
+    a.c0 = ctx->c0.p;
+    a.A0 = ctx->A0.p;
+    a.lb = ctx->lb.p;
+    a.ub = ctx->ub.p;
+    a.bnd32 = ctx->bnd32.p;
+    a.row_ptr = ctx->rowptr.p;
+    a.col_idx = ctx->colidx.p;
+    a.val = ctx->val.p;
+    a.N = ctx->N.p;
+    a.out = d_points_out;
+    a.ld_out = ld_out;
+    a.seed = seed;
+    a.chain_offset = chain_offset;
+    a.check_period = ctx->opt.check_period;
+    a.max_attempts = ctx->opt.max_attempts;
+    a.centre_offset = ctx->opt.centre_offset;
+    a.exact_ratio = ctx->opt.exact_ratio;
+    a.final_project = ctx->opt.mode == ACHR_MODE_FEASIBLE ? 1 : 0;
+    a.residual_tol = ctx->opt.residual_tol;
+    a.max_min_tol = ctx->opt.max_min_tol;
+    a.u_tol = ctx->opt.u_tol;
+    a.d_tol = ctx->opt.d_tol;
+    a.feasibility_tol = ctx->opt.feasibility_tol;
+    a.counters = ctx->counters.p;
+    ACHR_CUDA_TRY(cudaMemsetAsync(ctx->counters.p, 0, sizeof(unsigned long long) * achr::CNT_SLOTS, s));
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (stats) {
+        ACHR_CUDA_TRY(cudaEventCreate(&e0));
+        ACHR_CUDA_TRY(cudaEventCreate(&e1));
+        ACHR_CUDA_TRY(cudaEventRecord(e0, s));
+    }
+    cudaError_t e = achr::launch_chains(a, ctx->opt.threads_per_chain, s);
+    if (e != cudaSuccess) {
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+        return cuda_fail(e, "chain kernel launch");
+    }
+    if (!stats) return ACHR_OK;
+    ACHR_CUDA_TRY(cudaEventRecord(e1, s));
+    ACHR_CUDA_TRY(cudaEventSynchronize(e1));
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return read_counters(ctx, stats, ms);
+}
+
+achr_status achr_sample(achr_ctx *ctx, uint64_t seed, uint64_t chain_offset, int32_t n_points, int32_t n_steps,
+                        double *points_out, achr_stats *stats) {
+    if (!ctx) return fail(ACHR_ERR_INVALID, "ctx is NULL");
+    if (n_points < 0 || n_steps < 0) return fail(ACHR_ERR_INVALID, "n_points and n_steps must be >= 0");
+    if (n_points > 0 && !points_out) return fail(ACHR_ERR_INVALID, "points_out is NULL");
+    const size_t need = (size_t)ctx->n * (size_t)n_points;
+    if (ctx->points.count < need) ACHR_CUDA_TRY(ctx->points.alloc(need));
+    achr_stats local;
+    achr_status st = achr_sample_device(ctx, seed, chain_offset, n_points, n_steps, ctx->points.p, n_points, nullptr,
+                                        stats ? stats : &local);
+    if (st != ACHR_OK) return st;
+    if (need) ACHR_CUDA_TRY(cudaMemcpy(points_out, ctx->points.p, sizeof(double) * need, cudaMemcpyDeviceToHost));
+    return ACHR_OK;
+}
+
+void achr_destroy(achr_ctx *ctx) { delete ctx; }
+
+}  // extern "C"

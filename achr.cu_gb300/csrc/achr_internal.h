@@ -1,0 +1,57 @@
+// Internal declarations shared by the sampler translation units.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace achr {
+
+// Counters kept in device memory while a sampling launch runs.
+enum CounterSlot {
+    CNT_ACCEPTED = 0,
+    CNT_REJECTED = 1,
+    CNT_CHECKS = 2,
+    CNT_REPROJ = 3,
+    CNT_STUCK = 4,
+    CNT_EXACT = 5,
+    CNT_FINAL_PROJ = 6,
+    CNT_MAXRES_BITS = 7,   // max ||S v||_inf of emitted points, as the bits of a non-negative double
+    CNT_MAXVIOL_BITS = 8,  // max bound violation of emitted points, same encoding
+    CNT_ERROR = 9,         // bit flags, ERR_*
+    CNT_SLOTS = 16
+};
+
+enum DeviceError : unsigned long long {
+    ERR_TMA_TIMEOUT = 1ull,
+};
+
+// Everything one chain-sampling launch reads (device pointers) and its scalars.
+struct ChainArgs {
+    int n, m, W, d;
+    int ldw;                    // leading dimension of the warmup matrix in doubles (even)
+    int P, T;
+    const double *warmup;       // ldw x W, column j = warmup point j
+    const double *c0;           // n: start point and initial centre
+    const double *A0;           // n: (W + centre_offset) * c0, the centre accumulator at step 0
+    const double *lb, *ub;      // n
+    const float4 *bnd32;        // n: (float lb, float ub, |lb - float lb|, |ub - float ub|), errors rounded up
+    const int *row_ptr;         // CSR of S (m + 1)
+    const int *col_idx;
+    const double *val;
+    const double *N;            // n x d column-major null-space basis (ld = n)
+    double *out;                // n x P row-major block: out[i * ld_out + p]
+    long long ld_out;
+    unsigned long long seed, chain_offset;
+    int check_period, max_attempts, centre_offset, exact_ratio;
+    int final_project;          // 1: project+clip emitted points whose residual exceeds feasibility_tol
+    double residual_tol, max_min_tol, u_tol, d_tol, feasibility_tol;
+    unsigned long long *counters;  // CNT_SLOTS entries
+};
+
+// Launch the persistent chain kernel; threads_per_chain = 0 picks by size.
+cudaError_t launch_chains(const ChainArgs &a, int threads_per_chain, cudaStream_t stream);
+
+// Shared-memory bytes and block size the launcher would use (for tests/tuning).
+int chain_block_size(int n, int threads_per_chain);
+size_t chain_smem_bytes(int n, int d, int ldw, int block);
+
+}  // namespace achr

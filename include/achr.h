@@ -1,0 +1,183 @@
+/*
+ * achr.h -- C ABI of the GB300 ACHR sampler (Artificial-Centering Hit-and-Run
+ * over the flux polytope {v : S v = 0, lb <= v <= ub}).
+ *
+ * Plain pointers and sizes only; every call returns an achr_status and never
+ * throws or exits.  achr_last_error() gives a message for the calling thread.
+ * One context owns device copies of one model and its warmup points on one GPU.
+ *
+ * Each entry point names the part of the reference program it replaces
+ * (ACHRcu/ACHRCuda.cu in marouenbg/ACHR.cu).  The reference exposes a CLI,
+ * not a library; the CLI built from this library (ACHRCuda) keeps its
+ * arguments and output files.
+ */
+#ifndef ACHR_GB300_H
+#define ACHR_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    ACHR_OK = 0,
+    ACHR_ERR_INVALID = 1,     /* bad argument or malformed input */
+    ACHR_ERR_CUDA = 2,        /* CUDA runtime / library failure */
+    ACHR_ERR_NOMEM = 3,       /* host or device allocation failed */
+    ACHR_ERR_IO = 4,          /* file could not be opened, read or written */
+    ACHR_ERR_PARSE = 5,       /* MPS or CSV content does not parse */
+    ACHR_ERR_NUMERIC = 6,     /* null space / solver failure */
+    ACHR_ERR_TIMEOUT = 7,     /* a bounded device-side wait ran out */
+    ACHR_ERR_UNSUPPORTED = 8  /* size or option outside what this build handles */
+} achr_status;
+
+/* Stoichiometric model: S as COO triplets (any order, duplicates summed),
+ * bounds per reaction.  Mirrors what the reference keeps from the MPS file:
+ * S, lb and ub only (ACHRCuda.cu:567-597, COO build :642-663). */
+typedef struct {
+    int32_t n_rxns;           /* n: columns of S */
+    int32_t n_mets;           /* m: rows of S */
+    int64_t nnz;
+    const int32_t *row;       /* nnz metabolite indices in [0, m) */
+    const int32_t *col;       /* nnz reaction indices in [0, n) */
+    const double *val;        /* nnz coefficients */
+    const double *lb;         /* n lower bounds (may be -inf) */
+    const double *ub;         /* n upper bounds (may be +inf) */
+} achr_model;
+
+/* Reprojection / warmup handling. */
+enum {
+    /* Reference semantics: warmups used as given; every check_period-th step
+     * x <- N (N^T x) in FP64 when max|S x| > residual_tol (ACHRCuda.cu:325-343). */
+    ACHR_MODE_REFERENCE = 0,
+    /* Same loop, but warmup points and centre are first projected onto null(S)
+     * in FP64 (warmup CSVs are %f-rounded, so S w != 0 at ~1e-6), and every
+     * emitted point is projected, clipped and verified against feasibility_tol. */
+    ACHR_MODE_FEASIBLE = 1
+};
+
+/* Null-space basis construction. */
+enum {
+    ACHR_NULL_SVD_STS = 0,    /* SVD of S^T S, cutoff n*sigma0*2.2204e-16 (ACHRCuda.cu:436-502) */
+    ACHR_NULL_SVD_S = 1       /* SVD of S itself (better conditioned), same cutoff rule on sigma(S) */
+};
+
+typedef struct {
+    int32_t mode;             /* ACHR_MODE_* (default REFERENCE) */
+    int32_t null_space;       /* ACHR_NULL_* (default SVD_STS) */
+    int32_t check_period;     /* residual check every k-th step (default 10, ACHRCuda.cu:325) */
+    int32_t max_attempts;     /* rejected redraws of one step before a chain stops (default 100000) */
+    int32_t centre_offset;    /* 0: centre weights of ACHRCuda.cu:347-348; 1: ACHRSamplerMOD.m:174 */
+    int32_t exact_ratio;      /* 1: evaluate every ratio-test candidate in FP64 (diagnostic, slower) */
+    int32_t threads_per_chain;/* 0: autotuned; else 32..1024, multiple of 32 */
+    int32_t reserved;
+    double residual_tol;      /* 1e-9 (ACHRCuda.cu:338) */
+    double max_min_tol;       /* 1e-9 (ACHRCuda.cu:505) */
+    double u_tol;             /* 1e-9 (ACHRCuda.cu:508) */
+    double d_tol;             /* 1e-14 (ACHRCuda.cu:512) */
+    double feasibility_tol;   /* 1e-8: ||S v||_inf bound for emitted points in FEASIBLE mode */
+} achr_options;
+
+typedef struct {
+    int64_t accepted;         /* accepted steps over all chains */
+    int64_t rejected;         /* rejected attempts (reference ACHRCuda.cu:316-319) */
+    int64_t checks;           /* residual checks performed */
+    int64_t reprojections;    /* reprojections triggered (max|Sx| > residual_tol) */
+    int64_t stuck_chains;     /* chains that stopped after max_attempts rejections */
+    int64_t exact_evals;      /* ratio-test candidates evaluated in FP64 */
+    int64_t final_projections;/* emitted points that needed the FEASIBLE-mode projection */
+    double max_residual;      /* max ||S v||_inf over emitted points (FEASIBLE mode) */
+    double max_bound_violation; /* max over emitted points of max(lb - v, v - ub, 0) */
+    double kernel_ms;         /* device time of the sampling launch(es) */
+} achr_stats;
+
+typedef struct achr_ctx achr_ctx;
+
+/* Fill *opt with the reference's constants (see field comments). */
+void achr_default_options(achr_options *opt);
+
+/* Build a context: upload S (CSR), bounds and the n x W column-major warmup
+ * matrix (point j at warmup + j*n), compute the null-space basis N and the
+ * warmup centre.  Replaces ACHRCuda.cu:642-729 (COO build and upload,
+ * computeKernelCuda :436-502, createCenterPt :414-434, buffer set-up). */
+achr_status achr_create(const achr_model *model, const double *warmup, int32_t n_warmup,
+                        const achr_options *opt, achr_ctx **out);
+
+/* Replace the context's null-space basis with a caller-supplied one (n x d,
+ * column-major, host memory).  The reference computes it internally
+ * (ACHRCuda.cu:698-704); this lets a caller pin N across implementations. */
+achr_status achr_set_null_space(achr_ctx *ctx, const double *N, int32_t d);
+
+/* Null-space dimension d and the basis itself (n x d column-major, host). */
+achr_status achr_get_null_space_dim(const achr_ctx *ctx, int32_t *d);
+achr_status achr_get_null_space(const achr_ctx *ctx, double *N_out);
+
+/* Centre of the warmup points as used by the sampler (n doubles, host). */
+achr_status achr_get_centre(const achr_ctx *ctx, double *centre_out);
+
+/* Run P independent chains of T accepted steps each and copy the final
+ * points to host memory, n x P row-major (row = reaction, column = chain),
+ * the layout of the reference's points array (ACHRCuda.cu:247, 743).
+ * Chains are numbered chain_offset .. chain_offset+P-1 in the random stream
+ * keyed by seed; file ii of the CLI uses chain_offset = ii*P.
+ * Replaces one iteration of the per-file loop, ACHRCuda.cu:736-743
+ * (stepPointProgress launch :741 and the device-to-host copy :743). */
+achr_status achr_sample(achr_ctx *ctx, uint64_t seed, uint64_t chain_offset, int32_t n_points,
+                        int32_t n_steps, double *points_out, achr_stats *stats);
+
+/* Same as achr_sample, but the output is device memory (n x P row-major,
+ * leading dimension ld_out >= P) and the work is queued on `stream`
+ * (a cudaStream_t; NULL = legacy default stream).  Returns after the launch
+ * is queued; stats (if non-NULL) are filled after synchronising the stream. */
+achr_status achr_sample_device(achr_ctx *ctx, uint64_t seed, uint64_t chain_offset, int32_t n_points,
+                               int32_t n_steps, double *d_points_out, int64_t ld_out, void *stream,
+                               achr_stats *stats);
+
+/* Release every device and host resource of the context. */
+void achr_destroy(achr_ctx *ctx);
+
+/* ---- Host input/output used by the ACHRCuda CLI (ACHRCuda.cu:558-689, 744-756) ---- */
+
+/* Parsed model owned by the library (free with achr_free_model). */
+typedef struct {
+    achr_model model;         /* pointers into the arrays below */
+    int32_t *row_buf, *col_buf;
+    double *val_buf, *lb_buf, *ub_buf;
+} achr_model_buf;
+
+/* Read a fixed-format MPS file and keep S, lb, ub, as the reference does with
+ * glp_read_mps(GLP_MPS_DECK) (ACHRCuda.cu:560-597).  The first N row is the
+ * objective and is dropped; RHS and RANGES are ignored. */
+achr_status achr_read_mps(const char *path, achr_model_buf *out);
+void achr_free_model(achr_model_buf *m);
+
+/* Read a warmup CSV (n lines of W comma-separated values, ACHRCuda.cu:387-412,
+ * 675-689) into a malloc'd n x W column-major matrix (free with achr_free).
+ * No line-length limit; rows or columns that disagree are an error. */
+achr_status achr_read_warmup_csv(const char *path, int32_t n_rxns, double **warmup_out, int32_t *n_warmup_out);
+
+/* Write an n x P row-major matrix as the reference's File<ii> does:
+ * one line per reaction, "%f" values separated by ',' (ACHRCuda.cu:744-756).
+ * Byte-identical to fprintf("%f") output; formats with `threads` host threads. */
+achr_status achr_write_points_csv(const char *path, const double *points, int32_t n_rxns,
+                                  int32_t n_points, int32_t threads);
+
+/* Format one value exactly as printf("%f") into buf (>= 320 bytes); returns length.
+ * Exposed for testing the writer against the C library. */
+int32_t achr_format_f(double v, char *buf);
+
+void achr_free(void *p);
+
+/* Message describing the last failure on the calling thread ("" if none). */
+const char *achr_last_error(void);
+
+/* Library version (major*10000 + minor*100 + patch). */
+int32_t achr_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ACHR_GB300_H */

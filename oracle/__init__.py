@@ -1,0 +1,156 @@
+"""CPU oracle of the ACHR sampling step -- TEST INFRASTRUCTURE ONLY.
+
+Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline and
+reference arms may import this package, and only as the checker or as the
+timed CPU reference.  The product (the CUDA library and the ACHRCuda CLI)
+never calls into it.
+
+PARITY UNPINNED: the reference sampler (ACHRcu/ACHRCuda.cu) cannot be built
+here (CUDA 13 rejects its device-side cudaDeviceSynchronize(), sm_37 is gone,
+GLPK and GSL are absent) and ships no golden outputs or known-answer tests.
+The restatement is pinned by the published Philox4x32-10 known-answer
+vectors, by an independent pure-Python restatement (tests/golden/make_golden.py)
+whose outputs are committed as fixtures, and by invariants.
+
+Contents:
+  achr_oracle.c      FP64 C restatement of the step loop (ACHRcu/ACHRCuda.cu:193-385)
+  reference_py.py    pure-Python/numpy restatement of the same loop and of
+                     computeKernelCuda / createCenterPt (:414-502)
+  warmup.py          restatement of VFWarmup/createWarmupPtsGLPK.c with scipy HiGHS
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+BUILD_DIR = HERE / "_build"
+LIB_PATH = BUILD_DIR / "liboracle.so"
+
+
+def build(force: bool = False) -> Path:
+    """Compile achr_oracle.c into _build/liboracle.so (gcc, OpenMP, no FP contraction)."""
+    src = HERE / "achr_oracle.c"
+    if not force and LIB_PATH.exists() and LIB_PATH.stat().st_mtime > src.stat().st_mtime:
+        return LIB_PATH
+    BUILD_DIR.mkdir(exist_ok=True)
+    cc = os.environ.get("CC", "gcc")
+    cmd = [cc, "-O2", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared", "-std=c11", str(src), "-o",
+           str(LIB_PATH), "-lm"]
+    res = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    if res.returncode != 0:
+        raise RuntimeError(f"oracle build failed: {' '.join(cmd)}\n{res.stdout}")
+    return LIB_PATH
+
+
+class _Problem(C.Structure):
+    _fields_ = [
+        ("n", C.c_int32), ("m", C.c_int32), ("n_warmup", C.c_int32),
+        ("warmup", C.POINTER(C.c_double)), ("lb", C.POINTER(C.c_double)), ("ub", C.POINTER(C.c_double)),
+        ("row_ptr", C.POINTER(C.c_int32)), ("col_idx", C.POINTER(C.c_int32)), ("val", C.POINTER(C.c_double)),
+        ("d", C.c_int32), ("N", C.POINTER(C.c_double)), ("centre", C.POINTER(C.c_double)),
+    ]
+
+
+class _Options(C.Structure):
+    _fields_ = [
+        ("check_period", C.c_int32), ("max_attempts", C.c_int32), ("centre_offset", C.c_int32),
+        ("threads", C.c_int32),
+        ("residual_tol", C.c_double), ("max_min_tol", C.c_double), ("u_tol", C.c_double), ("d_tol", C.c_double),
+    ]
+
+
+class _Stats(C.Structure):
+    _fields_ = [("accepted", C.c_int64), ("rejected", C.c_int64), ("checks", C.c_int64),
+                ("reprojections", C.c_int64), ("stuck_chains", C.c_int64)]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = build()
+        h = C.CDLL(str(path))
+        h.oracle_philox4x32_10.argtypes = [C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]
+        h.oracle_philox4x32_10.restype = None
+        h.oracle_warmup_index.argtypes = [C.c_uint64, C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32]
+        h.oracle_warmup_index.restype = C.c_uint32
+        h.oracle_step_uniform.argtypes = [C.c_uint64, C.c_uint64, C.c_uint32]
+        h.oracle_step_uniform.restype = C.c_double
+        h.oracle_sample.argtypes = [C.POINTER(_Problem), C.POINTER(_Options), C.c_uint64, C.c_uint64, C.c_int32,
+                                    C.c_int32, C.POINTER(C.c_double), C.POINTER(_Stats)]
+        h.oracle_sample.restype = C.c_int
+        h.oracle_centre.argtypes = [C.c_int32, C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        h.oracle_centre.restype = None
+        _lib = h
+    return _lib
+
+
+def philox(ctr, key):
+    c = (C.c_uint32 * 4)(*[int(x) & 0xFFFFFFFF for x in ctr])
+    k = (C.c_uint32 * 2)(*[int(x) & 0xFFFFFFFF for x in key])
+    o = (C.c_uint32 * 4)()
+    lib().oracle_philox4x32_10(c, k, o)
+    return [int(x) for x in o]
+
+
+def warmup_index(seed, chain, step, attempt, W):
+    return int(lib().oracle_warmup_index(seed, chain, step, attempt, W))
+
+
+def step_uniform(seed, chain, step):
+    return float(lib().oracle_step_uniform(seed, chain, step))
+
+
+def csr(n_mets, row, col, val):
+    """CSR of S from COO (duplicates summed, zeros dropped), rows then columns ascending."""
+    S = {}
+    for r, c, v in zip(np.asarray(row).tolist(), np.asarray(col).tolist(), np.asarray(val).tolist()):
+        S[(r, c)] = S.get((r, c), 0.0) + v
+    keys = sorted(k for k, v in S.items() if v != 0.0)
+    row_ptr = np.zeros(n_mets + 1, dtype=np.int32)
+    for r, _ in keys:
+        row_ptr[r + 1] += 1
+    row_ptr = np.cumsum(row_ptr).astype(np.int32)
+    col_idx = np.array([c for _, c in keys], dtype=np.int32)
+    vals = np.array([S[k] for k in keys], dtype=np.float64)
+    return row_ptr, col_idx, vals
+
+
+def centre(warmup):
+    w = np.asfortranarray(np.asarray(warmup, dtype=np.float64))
+    n, W = w.shape
+    out = np.zeros(n)
+    lib().oracle_centre(n, W, w.ctypes.data_as(C.POINTER(C.c_double)), out.ctypes.data_as(C.POINTER(C.c_double)))
+    return out
+
+
+def sample(model, warmup, N, seed, n_points, n_steps, chain_offset=0, check_period=10, max_attempts=100000,
+           centre_offset=0, threads=0, residual_tol=1e-9, max_min_tol=1e-9, u_tol=1e-9, d_tol=1e-14,
+           centre_point=None):
+    """Run the C oracle.  model: object with n_rxns, n_mets, row, col, val, lb, ub.
+    warmup: (n, W); N: (n, d).  Returns ((n, P) points, stats dict)."""
+    n = model.n_rxns
+    w = np.asfortranarray(np.asarray(warmup, dtype=np.float64))
+    Nf = np.asfortranarray(np.asarray(N, dtype=np.float64).reshape(n, -1))
+    rp, ci, vv = csr(model.n_mets, model.row, model.col, model.val)
+    lb = np.ascontiguousarray(model.lb, dtype=np.float64)
+    ub = np.ascontiguousarray(model.ub, dtype=np.float64)
+    c0 = centre(w) if centre_point is None else np.ascontiguousarray(centre_point, dtype=np.float64)
+    dp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))  # noqa: E731
+    ip = lambda a: a.ctypes.data_as(C.POINTER(C.c_int32))  # noqa: E731
+    pb = _Problem(n, model.n_mets, w.shape[1], dp(w), dp(lb), dp(ub), ip(rp), ip(ci), dp(vv), Nf.shape[1], dp(Nf),
+                  dp(c0))
+    op = _Options(check_period, max_attempts, centre_offset, threads, residual_tol, max_min_tol, u_tol, d_tol)
+    out = np.zeros((n, n_points))
+    st = _Stats()
+    rc = lib().oracle_sample(C.byref(pb), C.byref(op), seed, chain_offset, n_points, n_steps, dp(out), C.byref(st))
+    if rc != 0:
+        raise RuntimeError(f"oracle_sample failed ({rc})")
+    return out, {k: getattr(st, k) for k, _ in st._fields_}
