@@ -105,33 +105,89 @@ def write_mps(path, n_mets, n_rxns, row, col, val, lb, ub, name="synthetic"):
         f.write("ENDATA\n")
 
 
-def chord_warmup(lb, ub, N, n_pts, seed=0):
-    """Warmup points for models too large for the LP restatement.
+def interior_point(S, lb, ub, cap=50.0):
+    """A feasible point with slack >= 1 on every reaction that can have it.
 
-    Stand-in for createWarmupPtsGLPK at genome scale: for random directions
-    N z (z ~ N(0, I)) through the feasible point 0, take the point where the
-    chord leaves the box (alternately at its far and near end, as the LP
-    warmup alternates max and min), then shrink every point toward the mean as
-    createWarmupPtsGLPK.c:283-284 does (0.33 x + 0.67 centre).  The points lie
-    in null(S) to FP64 rounding.
+    One LP (HiGHS interior point): maximise sum(y) subject to S v = 0,
+    y_i <= v_i - lb_i, y_i <= ub_i - v_i, 0 <= y_i <= cap.  Reactions left with
+    y_i = 0 cannot leave their bound (blocked).  The LP solution is then moved
+    back onto {S v = 0} with the blocked reactions held fixed (LSQR on S).
+    Returns (v0, blocked_mask).
     """
+    import scipy.sparse as sp
+    from scipy.optimize import linprog
+    from scipy.sparse.linalg import lsqr
+
+    S = sp.csr_matrix(S)
+    m, n = S.shape
+    eye = sp.identity(n, format="csr")
+    A_ub = sp.vstack([sp.hstack([-eye, eye]), sp.hstack([eye, eye])]).tocsr()
+    b_ub = np.concatenate([-lb, ub])
+    A_eq = sp.hstack([S, sp.csr_matrix((m, n))]).tocsr()
+    bounds = [(lo, up) for lo, up in zip(lb, ub)] + [(0.0, cap)] * n
+    c = np.concatenate([np.zeros(n), -np.ones(n)])
+    res = linprog(c, A_ub=A_ub, b_ub=b_ub, A_eq=A_eq, b_eq=np.zeros(m), bounds=bounds, method="highs-ipm")
+    if res.status != 0:
+        raise RuntimeError(f"interior-point LP failed: {res.message}")
+    v0 = res.x[:n].copy()
+    blocked = res.x[n:] < 0.5e-3 * cap
+    v0[blocked] = np.where(np.abs(v0[blocked] - lb[blocked]) <= np.abs(v0[blocked] - ub[blocked]), lb[blocked],
+                           ub[blocked])
+    free = ~blocked
+    SF = S[:, free].tocsr()
+    for _ in range(3):
+        r = S @ v0
+        delta = lsqr(SF, r, atol=1e-15, btol=1e-15, iter_lim=20000)[0]
+        v0[free] -= delta
+    v0 = np.minimum(np.maximum(v0, lb), ub)
+    return v0, blocked
+
+
+def interior_chord_warmup(S, lb, ub, n_pts, seed=0, null_space=None):
+    """Warmup points for genome-scale models (stand-in for createWarmupPtsGLPK).
+
+    The reference generates one LP solution per warmup point (FVA extremes,
+    VFWarmup/createWarmupPtsGLPK.c:100-173); at 3742 reactions one LP takes
+    about 5 s here, so 7484 of them are out of reach.  Instead: from the
+    interior point v0 (one LP), follow random directions P_F g (g ~ N(0, I),
+    P_F the orthogonal projector onto the null space of S restricted to the
+    non-blocked reactions) to where each chord leaves the box, alternating the
+    far and near end as the reference alternates max and min; clip, and shrink
+    toward the mean with 0.33 x + 0.67 centre (createWarmupPtsGLPK.c:283-284).
+    The points satisfy S w = 0 to FP64 rounding.  null_space(S_F) -> basis
+    may be supplied; the default uses numpy's symmetric eigensolver.
+    """
+    S = np.asarray(S.todense() if hasattr(S, "todense") else S, dtype=np.float64)
+    lb = np.asarray(lb, dtype=np.float64)
+    ub = np.asarray(ub, dtype=np.float64)
+    v0, blocked = interior_point(S, lb, ub)
+    free = np.flatnonzero(~blocked)
+    SF = S[:, free]
+    if null_space is None:
+        lam, V = np.linalg.eigh(SF.T @ SF)
+        tol = len(free) * max(abs(lam).max(), 0.0) * 2.2204e-16
+        NF = V[:, np.abs(lam) < tol]
+    else:
+        NF = null_space(SF)
     rng = np.random.default_rng(seed)
-    n, d = N.shape
-    pts = np.zeros((n, n_pts))
-    block = 512
+    n = S.shape[1]
+    pts = np.empty((n, n_pts))
+    lbF, ubF, vF = lb[free], ub[free], v0[free]
+    block = 1024
     for j0 in range(0, n_pts, block):
         j1 = min(n_pts, j0 + block)
-        Z = rng.standard_normal((d, j1 - j0))
-        D = N @ Z  # n x b directions
+        G = rng.standard_normal((len(free), j1 - j0))
+        D = NF @ (NF.T @ G)
         with np.errstate(divide="ignore", invalid="ignore"):
-            up = np.where(D > 0, ub[:, None] / D, np.where(D < 0, lb[:, None] / D, np.inf))
-            lo = np.where(D > 0, lb[:, None] / D, np.where(D < 0, ub[:, None] / D, -np.inf))
+            up = np.where(D > 0, (ubF - vF)[:, None] / D, np.where(D < 0, (lbF - vF)[:, None] / D, np.inf))
+            lo = np.where(D > 0, (lbF - vF)[:, None] / D, np.where(D < 0, (ubF - vF)[:, None] / D, -np.inf))
         tmax = np.min(up, axis=0)
         tmin = np.max(lo, axis=0)
-        sign = np.where((np.arange(j0, j1) % 2) == 1, 1.0, 0.0)
-        t = sign * tmax + (1.0 - sign) * tmin
+        far = (np.arange(j0, j1) % 2) == 1
+        t = np.where(far, tmax, tmin)
         t = np.where(np.isfinite(t), t, 0.0)
-        pts[:, j0:j1] = D * t[None, :]
+        pts[:, j0:j1] = v0[:, None]
+        pts[free, j0:j1] = vF[:, None] + D * t[None, :]
     pts = np.minimum(np.maximum(pts, lb[:, None]), ub[:, None])
     centre = pts.mean(axis=1)
     return pts * 0.33 + 0.67 * centre[:, None]

@@ -1,0 +1,336 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 ACHR sampler: chain-steps/s on the genome-scale workload.
+
+Workload ("genome"): seeded synthetic model 2766 metabolites x 3742 reactions
+(each reaction touches 2-6 metabolites, coefficients in {-2,-1,1,2}, 30%
+irreversible, 150 exchange reactions bounded +-20), 7484 = 2n warmup points,
+100,000 chains x 2000 steps, plain ACHR in FP64 with the reference's
+semantics.  One "step" of this benchmark is one full sampling launch of that
+workload (2e8 chain-steps).  The warmup matrix (224 MB) exceeds the 129 MB L2,
+so no explicit L2 flush is done between timed launches.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference] [--workload genome|small]
+
+Prints one JSON line on rank 0.  --impl reference times the CPU restatement of
+the reference's sampling loop (the oracle, OpenMP over chains, all host
+threads) on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import csv
+import io
+import json
+import os
+import re
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "chain-steps/s"
+WORKLOADS = {
+    # name: (spec attribute, chains, steps)
+    "genome": ("GENOME", 100_000, 2000),
+    "small": ("SMALL", 1000, 1000),
+}
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="genome")
+    ap.add_argument("--seed", type=int, default=20261203)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target length of the CPU baseline sample")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def load_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profile_traffic_per_chain_step(workload):
+    """DRAM bytes per chain-step from the committed ncu summary of the chain kernel."""
+    p = ROOT / "profiles" / f"chain_kernel_{workload}.md"
+    if not p.exists():
+        return None
+    m = re.search(r"dram_bytes_per_chain_step:\s*([0-9.eE+-]+)", p.read_text())
+    return float(m.group(1)) if m else None
+
+
+def build_inputs(workload, pkg, synth):
+    """Model arrays, dense S and warmup points (numpy; identical for both arms).
+    Cached under /tmp so the two arms of one run share the set-up work."""
+    spec_name, P, T = WORKLOADS[workload]
+    spec = getattr(synth, spec_name)
+    cache = Path("/tmp") / f"achr_bench_{workload}_{spec.seed}_v2.npz"
+    row, col, val, lb, ub = synth.make_model(spec)
+    S = synth.dense(spec.n_mets, spec.n_rxns, row, col, val)
+    W = 2 * spec.n_rxns
+    if cache.exists():
+        warm = np.load(cache)["warm"]
+    else:
+        warm = synth.interior_chord_warmup(S, lb, ub, W, seed=spec.seed + 17)
+        np.savez(cache, warm=warm)
+    model = pkg.HostModel(spec.n_rxns, spec.n_mets, row, col, val, lb, ub)
+    return spec, model, S, warm, P, T
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms while running."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.proc = None
+        self.gpu_index = gpu_index
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu_index}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, ValueError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+            out, _ = self.proc.communicate()
+        rows = [r for r in csv.reader(io.StringIO(out)) if len(r) >= 9]
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].strip().replace(".", "").isdigit()]
+        smax = [float(r[2]) for r in rows if r[2].strip().replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if "Active" in r[5 + k] and "Not" not in r[5 + k]})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def cpu_baseline(oracle, model, warm, N, T, seed, target_s):
+    """Time the oracle (all host threads) on a bounded chain sample of the workload."""
+    threads = os.cpu_count() or 1
+    probe_chains, probe_steps = threads, 20
+    t0 = time.perf_counter()
+    oracle.sample(model, warm, N, seed, probe_chains, probe_steps, chain_offset=10**9, threads=threads)
+    per_round = (time.perf_counter() - t0) / probe_steps  # seconds per step for `threads` chains
+    rounds = max(1, int(target_s / max(per_round * T, 1e-9)))
+    P = threads * rounds
+    t0 = time.perf_counter()
+    _, st = oracle.sample(model, warm, N, seed, P, T, threads=threads)
+    el = time.perf_counter() - t0
+    return {"value": st["accepted"] / el, "unit": METRIC, "cores": threads, "kind": "port",
+            "sample": f"{P} chains x {T} steps of the same workload ({st['accepted']} chain-steps, {el:.1f} s)"}
+
+
+def oracle_null_space(S):
+    """Null-space basis by the reference's rule (S^T S spectrum, cutoff n*s0*2.2204e-16), numpy eigh."""
+    n = S.shape[1]
+    lam, V = np.linalg.eigh(S.T @ S)
+    tol = n * np.abs(lam).max() * 2.2204e-16
+    keep = np.abs(lam) < tol
+    return V[:, keep] if keep.any() else V
+
+
+def run_reference(args):
+    rank, world, _ = dist_info()
+    if rank != 0:
+        return 0
+    import __graft_entry__ as ge
+    import oracle
+
+    pkg = ge.load_package()
+    import importlib
+    synth = importlib.import_module("achr_gb300.synthetic")
+    oracle.build()
+    spec, model, S, warm, P, T = build_inputs(args.workload, pkg, synth)
+    N = oracle_null_space(S)
+    threads = os.cpu_count() or 1
+    # each step: a bounded chain sample of the workload sized to ~8 s
+    t0 = time.perf_counter()
+    oracle.sample(model, warm, N, args.seed, threads, 20, chain_offset=10**9, threads=threads)
+    per_round = (time.perf_counter() - t0) / 20
+    rounds = max(1, int(8.0 / max(per_round * T, 1e-9)))
+    Pstep = threads * rounds
+    for w in range(args.warmup):
+        oracle.sample(model, warm, N, args.seed + w, threads, min(T, 50), threads=threads)
+    times, acc = [], 0
+    for k in range(args.steps):
+        t0 = time.perf_counter()
+        _, st = oracle.sample(model, warm, N, args.seed + 100 + k, Pstep, T, chain_offset=k * Pstep, threads=threads)
+        times.append(time.perf_counter() - t0)
+        acc += st["accepted"]
+    total = sum(times)
+    value = acc / total
+    line = {
+        "metric": METRIC, "value": value, "unit": METRIC, "impl": "reference", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"{args.workload}: {spec.n_mets}x{spec.n_rxns} synthetic model, W={warm.shape[1]}, "
+                               f"{P} chains x {T} steps (CPU step = {Pstep} chains x {T} steps)",
+                   "parallelism": f"openmp{threads}"},
+        "cpu_baseline": {"value": value, "unit": METRIC, "cores": threads, "kind": "port",
+                         "sample": f"{Pstep} chains x {T} steps per step, {args.steps} steps"},
+        "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_gpu(args):
+    rank, world, local = dist_info()
+    import torch
+
+    if not torch.cuda.is_available():
+        raise SystemExit("bench.py: no CUDA device")
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    import importlib
+
+    import __graft_entry__ as ge
+
+    pkg = ge.load_package()
+    pkg.lib()
+    synth = importlib.import_module("achr_gb300.synthetic")
+    spec, model, S, warm, P, T = build_inputs(args.workload, pkg, synth)
+    n = spec.n_rxns
+    chain_base = rank * P  # weak scaling: every rank runs its own P chains
+
+    t_setup = time.perf_counter()
+    smp = pkg.Sampler(model, warm)
+    setup_s = time.perf_counter() - t_setup
+    stream = torch.cuda.current_stream()
+    out = torch.empty((n, P), dtype=torch.float64, device="cuda")
+
+    stats = None
+    for w in range(args.warmup):
+        st = smp.sample_device(P, T, out.data_ptr(), P, stream.cuda_stream, seed=args.seed + w,
+                               chain_offset=chain_base, with_stats=(w == args.warmup - 1))
+        stats = st or stats
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    evs = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+    torch.cuda.synchronize()
+    evs[0].record(stream)
+    for k in range(args.steps):
+        smp.sample_device(P, T, out.data_ptr(), P, stream.cuda_stream, seed=args.seed + 1000 + k,
+                          chain_offset=chain_base)
+        evs[k + 1].record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    per_launch = [evs[k].elapsed_time(evs[k + 1]) for k in range(args.steps)]
+    ms = sum(per_launch) / args.steps
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+        torch.distributed.barrier()
+    chain_steps = P * T
+    value = world * chain_steps / (ms * 1e-3)
+
+    peak, peak_kind = load_peaks()
+    alg_bytes = synth.ideal_bytes_per_chain_step(n) * chain_steps
+    achieved = alg_bytes / (ms * 1e-3) / 1e9
+    tpcs = profile_traffic_per_chain_step(args.workload)
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": (tpcs * chain_steps) if tpcs is not None else None,
+                "peak_source": f"{peak_kind} hbm_gbs", "algorithmic_bytes_per_launch": alg_bytes}
+
+    # End to end through the public API with host buffers: set-up from pinned host
+    # model + warmup (H2D, null space, centre), sampling, D2H of every point.
+    e2e = None
+    if not args.no_e2e:
+        warm_pinned = torch.from_numpy(np.asfortranarray(warm).T.copy()).pin_memory()  # (W, n) = column-major n x W
+        host_out = torch.empty((n, P), dtype=torch.float64).pin_memory()
+        wnp = warm_pinned.numpy().T  # (n, W) view, Fortran order over pinned memory
+        e2e_times = []
+        for k in range(max(1, args.steps)):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            with pkg.Sampler(model, wnp) as s2:
+                s2.sample(P, T, seed=args.seed + 2000 + k, chain_offset=chain_base, out=host_out.numpy())
+            torch.cuda.synchronize()
+            e2e_times.append(time.perf_counter() - t0)
+        e2e_s = max(sum(e2e_times) / len(e2e_times), 1e-9)
+        h2d = warm.size * 8 + len(model.row) * 16 + n * 16
+        e2e = {"value": world * chain_steps / e2e_s, "unit": METRIC, "h2d_bytes_per_step": int(h2d),
+               "d2h_bytes_per_step": int(n * P * 8), "seconds_per_step": e2e_s}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        import oracle
+
+        oracle.build()
+        Nb = smp.null_space()
+        cpu = cpu_baseline(oracle, model, warm, Nb, T, args.seed, args.cpu_seconds)
+
+    line = {
+        "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"{args.workload}: {spec.n_mets}x{spec.n_rxns} synthetic model, W={warm.shape[1]}, "
+                               f"{P} chains x {T} steps per GPU, mode=reference",
+                   "global_batch": world * P, "seq_len": T, "parallelism": f"chains sharded over {world} GPU(s)",
+                   "l2": "inputs exceed L2 (warmup matrix 224 MB > 129 MB); no flush"},
+        "gpu_launches": args.steps,
+        "roofline": roofline,
+        "cpu_baseline": cpu,
+        "e2e": e2e,
+        "clocks": clk,
+        "sampler": {"null_dim": smp.null_dim, "setup_s": setup_s,
+                    **({k: stats[k] for k in ("accepted", "rejected", "checks", "reprojections", "stuck_chains",
+                                              "exact_evals", "max_residual", "max_bound_violation")} if stats else {})},
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    smp.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())
