@@ -66,11 +66,12 @@ struct DevBuf {
     }
 };
 
-// Float image of a bound with a rounded-up conversion error (used by the FP32
-// ratio-test brackets of the chain kernel).
+// FP32 image of a bound for the chain kernel's brackets: round to nearest, an
+// infinite bound becomes a finite stand-in (keeps the bracket arithmetic free
+// of inf - inf); err is the conversion error rounded up (0 for infinities).
 void f32_bound(double v, float &f, float &err) {
     if (std::isinf(v)) {
-        f = (float)v;
+        f = v > 0 ? 3.0e38f : -3.0e38f;
         err = 0.0f;
         return;
     }
@@ -79,6 +80,18 @@ void f32_bound(double v, float &f, float &err) {
     float ef = (float)e;
     if ((double)ef < e) ef = std::nextafter(ef, INFINITY);
     err = ef;
+}
+
+float f32_up(double v) {
+    float f = (float)v;
+    if ((double)f < v) f = std::nextafter(f, INFINITY);
+    return f;
+}
+
+float f32_down(double v) {
+    float f = (float)v;
+    if ((double)f > v) f = std::nextafter(f, -INFINITY);
+    return f;
 }
 
 __global__ void centre_kernel(int n, int W, int ldw, const double *__restrict__ warmup, int centre_offset,
@@ -96,14 +109,16 @@ __global__ void centre_kernel(int n, int W, int ldw, const double *__restrict__ 
 }  // namespace
 
 struct achr_ctx {
-    int n = 0, m = 0, W = 0, d = 0, ldw = 0;
+    int n = 0, m = 0, W = 0, d = 0, ldw = 0, np = 0;
+    float bound_err = 0.0f;
     int device = 0;
     achr_options opt{};
     std::vector<double> h_lb, h_ub;
     std::vector<int> h_rowptr, h_colidx;
     std::vector<double> h_val;
-    DevBuf<double> warmup, c0, A0, lb, ub, val, N, points;
-    DevBuf<float4> bnd32;
+    DevBuf<double> warmup, c0, A0, val, N, points;
+    DevBuf<double2> lbub;
+    DevBuf<float2> bnd;
     DevBuf<int> rowptr, colidx;
     DevBuf<unsigned long long> counters;
 };
@@ -144,9 +159,9 @@ achr_status validate_options(const achr_options &o) {
     if (o.check_period <= 0) return fail(ACHR_ERR_INVALID, "check_period must be positive");
     if (o.max_attempts <= 0) return fail(ACHR_ERR_INVALID, "max_attempts must be positive");
     if (o.centre_offset != 0 && o.centre_offset != 1) return fail(ACHR_ERR_INVALID, "centre_offset must be 0 or 1");
-    if (o.threads_per_chain != 0 &&
-        (o.threads_per_chain < 32 || o.threads_per_chain > 512 || o.threads_per_chain % 32 != 0))
-        return fail(ACHR_ERR_INVALID, "threads_per_chain must be 0 or a multiple of 32 in [32, 512]");
+    if (o.threads_per_chain != 0 && o.threads_per_chain != 32 && o.threads_per_chain != 64 &&
+        o.threads_per_chain != 128 && o.threads_per_chain != 256 && o.threads_per_chain != 512)
+        return fail(ACHR_ERR_INVALID, "threads_per_chain must be 0, 32, 64, 128, 256 or 512");
     if (!(o.residual_tol >= 0) || !(o.max_min_tol >= 0) || !(o.u_tol >= 0) || !(o.d_tol >= 0) ||
         !(o.feasibility_tol >= 0))
         return fail(ACHR_ERR_INVALID, "tolerances must be non-negative");
@@ -350,20 +365,31 @@ achr_status achr_create(const achr_model *model, const double *warmup, int32_t n
     }
     for (int r = 0; r < m; ++r) ctx->h_rowptr[(size_t)r + 1] += ctx->h_rowptr[(size_t)r];
 
-    std::vector<float4> b32(n);
+    // Per-reaction arrays are padded to the kernel's block size x elements per
+    // thread; padding entries are fixed at 0 (lb = ub = 0) and never move.
+    const int np = achr::chain_padded_length(n, opt.threads_per_chain);
+    if (np == 0) return fail(ACHR_ERR_UNSUPPORTED, "no chain-kernel configuration for n_rxns with this threads_per_chain");
+    ctx->np = np;
+    // Padding reactions have lb = ub = 0 in FP64 and the FP32 box (-1, 1), so
+    // their (zero) coordinate is never a candidate and never needs a clip.
+    std::vector<float2> b32((size_t)np, make_float2(-1.0f, 1.0f));
+    std::vector<double2> lu((size_t)np, make_double2(0.0, 0.0));
+    float berr = 0.0f;
     for (int i = 0; i < n; ++i) {
         if (!(model->lb[i] <= model->ub[i])) return fail(ACHR_ERR_INVALID, "lb > ub or NaN bound at reaction " + std::to_string(i));
         float lf, le, uf, ue;
         f32_bound(model->lb[i], lf, le);
         f32_bound(model->ub[i], uf, ue);
-        b32[i] = make_float4(lf, uf, le, ue);
+        b32[i] = make_float2(lf, uf);
+        berr = std::max(berr, std::max(le, ue));
+        lu[i] = make_double2(model->lb[i], model->ub[i]);
     }
+    ctx->bound_err = berr;
     for (int64_t k = 0; k < (int64_t)n * n_warmup; ++k)
         if (!std::isfinite(warmup[k])) return fail(ACHR_ERR_INVALID, "warmup points must be finite");
 
-    ACHR_CUDA_TRY(ctx->lb.upload(model->lb, n));
-    ACHR_CUDA_TRY(ctx->ub.upload(model->ub, n));
-    ACHR_CUDA_TRY(ctx->bnd32.upload(b32.data(), n));
+    ACHR_CUDA_TRY(ctx->lbub.upload(lu.data(), np));
+    ACHR_CUDA_TRY(ctx->bnd.upload(b32.data(), np));
     ACHR_CUDA_TRY(ctx->rowptr.upload(ctx->h_rowptr.data(), ctx->h_rowptr.size()));
     ACHR_CUDA_TRY(ctx->colidx.upload(ctx->h_colidx.data(), ctx->h_colidx.size()));
     ACHR_CUDA_TRY(ctx->val.upload(ctx->h_val.data(), ctx->h_val.size()));
@@ -398,8 +424,10 @@ achr_status achr_create(const achr_model *model, const double *warmup, int32_t n
     if (st != ACHR_OK) return st;
 
     // Centre of the warmup points and the centre accumulator.
-    ACHR_CUDA_TRY(ctx->c0.alloc(n));
-    ACHR_CUDA_TRY(ctx->A0.alloc(n));
+    ACHR_CUDA_TRY(ctx->c0.alloc(np));
+    ACHR_CUDA_TRY(ctx->A0.alloc(np));
+    ACHR_CUDA_TRY(cudaMemset(ctx->c0.p, 0, sizeof(double) * np));
+    ACHR_CUDA_TRY(cudaMemset(ctx->A0.p, 0, sizeof(double) * np));
     centre_kernel<<<(n + 127) / 128, 128>>>(n, n_warmup, ctx->ldw, ctx->warmup.p, opt.centre_offset, ctx->c0.p,
                                             ctx->A0.p);
     ACHR_CUDA_TRY(cudaGetLastError());
@@ -447,15 +475,20 @@ achr_status achr_sample_device(achr_ctx *ctx, uint64_t seed, uint64_t chain_offs
     a.m = ctx->m;
     a.W = ctx->W;
     a.d = ctx->d;
+    a.np = ctx->np;
     a.ldw = ctx->ldw;
     a.P = n_points;
     a.T = n_steps;
     a.warmup = ctx->warmup.p;
     a.c0 = ctx->c0.p;
     a.A0 = ctx->A0.p;
-    a.lb = ctx->lb.p;
-    a.ub = ctx->ub.p;
-    a.bnd32 = ctx->bnd32.p;
+    a.lbub = ctx->lbub.p;
+    a.bnd = ctx->bnd.p;
+    a.bound_err = ctx->bound_err;
+    a.dtol_hi = f32_up(ctx->opt.d_tol) * (1.0f + 9.5367431640625e-07f);
+    a.dtol_lo = f32_down(ctx->opt.d_tol) * (1.0f - 9.5367431640625e-07f);
+    a.utol32 = (float)ctx->opt.u_tol;
+    a.mmt32 = (float)ctx->opt.max_min_tol;
     a.row_ptr = ctx->rowptr.p;
     a.col_idx = ctx->colidx.p;
     a.val = ctx->val.p;

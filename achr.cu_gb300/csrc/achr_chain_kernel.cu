@@ -10,17 +10,22 @@
 //   * The chain's point x and centre accumulator A = (W + t) c live in shared
 //     memory for all T steps; only the warmup column w_r is read from HBM/L2
 //     each step, staged into shared memory by a 1-D TMA bulk copy
-//     (cp.async.bulk + mbarrier) that is issued one step ahead.
+//     (cp.async.bulk + mbarrier) issued one step ahead.
 //   * GB300's FP64 pipe issues about 1.6 DFMA per clock per SM, 72x less than
-//     FP32.  Per element and accepted step the kernel therefore spends three
-//     FP64 pipe operations on the update (d = w - A/(W+t), x += s d, A += x),
-//     one for the norm, and none for the ratio test: the bound distances and
-//     ratios are bracketed in FP32 with rigorous error bounds, and only the
-//     candidates whose bracket can hold the minimum are evaluated in FP64.
-//   * The ratio test uses the unnormalised direction d (t/||d|| is what the
-//     update needs), so no per-element FP64 division remains.
-//   * Reductions are warp shuffles plus one shared-memory exchange; summation
-//     order is fixed, so a launch is bitwise repeatable.
+//     FP32, and FP64 compares cost as much as FMAs.  Per element and accepted
+//     step the kernel spends exactly three FP64 pipe instructions
+//     (d = w - A/(W+t), x += s d, A += x).  The norm is summed in FP32 (it only
+//     feeds tolerance tests, which carry margins and fall back to FP64 when a
+//     margin is not enough); the ratio test brackets every bound distance and
+//     ratio in FP32 with rigorous error bounds and evaluates in FP64 only the
+//     coordinates whose bracket can hold the minimum; clipping and the min/max
+//     reductions compare FP64 values as integers (order-preserving keys).
+//   * Per-step scalars (warmup index, step uniform, 1/(W+t)) come from a
+//     shared-memory table that the CTA refills once every BD steps.
+//   * The element loops are unrolled over compile-time BD x EPT with arrays
+//     padded to that length, so no loop carries a bounds test.
+//   * Reductions are warp shuffles plus one shared-memory exchange in a fixed
+//     order, so a launch is bitwise repeatable.
 #include <cfloat>
 #include <cmath>
 
@@ -35,20 +40,75 @@ constexpr float kTiny = 2.350988701644575e-38f;        // 2^-125: absolute error
 constexpr float kUp = 1.0f + 9.5367431640625e-07f;     // 1 + 2^-20
 constexpr float kDn = 1.0f - 9.5367431640625e-07f;     // 1 - 2^-20
 constexpr float kAdUp = 1.0f + 4.76837158203125e-07f;  // 1 + 2^-21
+constexpr float kNormUp = 1.0f + 1e-5f;                // FP32 norm relative error margin
+constexpr float kNormDn = 1.0f - 1e-5f;
 constexpr unsigned long long kWaitNs = 2000000000ull;  // bounded mbarrier wait: 2 s
+constexpr unsigned long long kInfBits = 0x7FF0000000000000ull;
 
-// FP64 -> FP32 rounding toward zero with integer operations only (no FP64
-// pipe).  |v - f| <= 2^-23 |f| + 2^-126; tiny values flush to signed zero,
-// overflow and inf map to inf.
+// FP64 -> FP32 rounding toward zero with integer operations only.
+// |v - f| <= 2^-23 |f| + 2^-126; tiny values flush to signed zero, overflow
+// and inf map to inf.
 __device__ __forceinline__ float f64_to_f32_rz(double v) {
     const unsigned hi = (unsigned)__double2hiint(v);
     const unsigned lo = (unsigned)__double2loint(v);
-    const unsigned sign = hi & 0x80000000u;
     const int fe = (int)((hi >> 20) & 0x7FFu) - 896;  // re-bias 1023 -> 127
     unsigned mag = ((unsigned)fe << 23) | ((hi & 0xFFFFFu) << 3) | (lo >> 29);
     mag = (fe <= 0) ? 0u : mag;
     mag = (fe >= 255) ? 0x7F800000u : mag;
-    return __uint_as_float(sign | mag);
+    return __uint_as_float((hi & 0x80000000u) | mag);
+}
+
+// Order-preserving integer key of a double (sign-magnitude -> two's
+// complement; -0 and +0 share key 0).  a < b  <=>  key(a) < key(b) for non-NaN.
+__device__ __forceinline__ long long order_key(double v) {
+    const long long b = __double_as_longlong(v);
+    const long long mag = b & 0x7FFFFFFFFFFFFFFFll;
+    return b < 0 ? -mag : mag;
+}
+
+// Exact clip of x to [lb, ub] (reference correctBounds, ACHRCuda.cu:198-202):
+// x itself when inside, else the bound, compared through integer keys.
+__device__ __forceinline__ double clip_exact(double x, double2 lu) {
+    const long long kx = order_key(x);
+    double r = x;
+    if (kx < order_key(lu.x)) r = lu.x;
+    if (kx > order_key(lu.y)) r = lu.y;
+    return r;
+}
+
+// (lb, ub) of one reaction.  A volatile load, so that the compiler keeps it
+// (and the FP64 work that depends on it) inside the rarely taken branches.
+// |v| and its bit pattern through integer operations (fabs on a double can be
+// issued to the FP64 pipe).
+__device__ __forceinline__ unsigned long long abs_bits(double v) {
+    return (unsigned long long)__double_as_longlong(v) & 0x7FFFFFFFFFFFFFFFull;
+}
+__device__ __forceinline__ double abs_int(double v) { return __longlong_as_double((long long)abs_bits(v)); }
+__device__ __forceinline__ bool positive_int(double v) {  // v > 0 for non-NaN v
+    const long long b = __double_as_longlong(v);
+    return b > 0;
+}
+
+// r[k] for a run-time k without indexing the register array dynamically.
+template <int EPT>
+__device__ __forceinline__ double pick(const double (&r)[EPT], int k) {
+    double v = r[0];
+#pragma unroll
+    for (int j = 1; j < EPT; ++j) v = (j == k) ? r[j] : v;
+    return v;
+}
+
+__device__ __forceinline__ double2 ld_lbub(const double2 *p) {
+    double2 v;
+    asm volatile("ld.global.nc.v2.f64 {%0, %1}, [%2];" : "=d"(v.x), "=d"(v.y) : "l"(p));
+    return v;
+}
+
+// FP32 test that x (as its truncation x32) lies strictly inside (lb, ub):
+// true only when the bracket arithmetic proves it; false means "test exactly".
+__device__ __forceinline__ bool surely_inside(float x32, float2 b, float berr) {
+    const float ex = fmaf(fabsf(x32), kErrK, kTiny + berr);
+    return (x32 - b.x) > ex && (b.y - x32) > ex;
 }
 
 __device__ __forceinline__ unsigned smem_addr(const void *p) {
@@ -111,220 +171,188 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, unsigned parity
     }
 }
 
-__device__ __forceinline__ double warp_sum(double v) {
-#pragma unroll
-    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    return v;
-}
-__device__ __forceinline__ double warp_max(double v) {
-#pragma unroll
-    for (int o = 16; o; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
-    return v;
-}
-__device__ __forceinline__ double warp_min(double v) {
-#pragma unroll
-    for (int o = 16; o; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
-    return v;
-}
-__device__ __forceinline__ float warp_minf(float v) {
-#pragma unroll
-    for (int o = 16; o; o >>= 1) v = fminf(v, __shfl_xor_sync(0xffffffffu, v, o));
-    return v;
-}
-__device__ __forceinline__ int warp_or(int v) {
-#pragma unroll
-    for (int o = 16; o; o >>= 1) v |= __shfl_xor_sync(0xffffffffu, v, o);
-    return v;
+__device__ __forceinline__ float rcp_approx(float x) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
 }
 
-// Shared-memory exchange slots of the block reductions.  Each reduction in a
-// step uses its own slots; a __syncthreads() separates two uses of one slot.
+template <class T>
+__device__ __forceinline__ T umin(T a, T b) {
+    return a < b ? a : b;
+}
+template <class T>
+__device__ __forceinline__ T umax(T a, T b) {
+    return a > b ? a : b;
+}
+
+__device__ __forceinline__ unsigned long long shfl_u64(unsigned long long v, int o) {
+    return __shfl_xor_sync(0xffffffffu, v, o);
+}
+
+// Shared-memory exchange slots, two sets selected by attempt parity so that
+// consecutive attempts never overwrite slots another warp may still read.
 struct RedSlots {
-    double sum[32];
-    float2 fmin2[32];
+    float sum1[32];
+    int flag1[32];
+    float2 min2[32];
     int flag2[32];
-    double2 dmin2[32];
+    ulonglong2 min3[32];
     int flag3[32];
-    double mx[32];
-    double viol[32];
+    unsigned long long max4[32];
+    double sum5[32];
 };
 
-__device__ __forceinline__ double block_sum(double v, double *slot, int lane, int warp, int nwarps) {
-    v = warp_sum(v);
-    if (lane == 0) slot[warp] = v;
-    __syncthreads();
-    double r = 0.0;
-    for (int w = 0; w < nwarps; ++w) r += slot[w];
-    return r;
-}
-
-__device__ __forceinline__ double block_max(double v, double *slot, int lane, int warp, int nwarps) {
-    v = warp_max(v);
-    if (lane == 0) slot[warp] = v;
-    __syncthreads();
-    double r = slot[0];
-    for (int w = 1; w < nwarps; ++w) r = fmax(r, slot[w]);
-    return r;
-}
-
-// FP32 bracket of one coordinate's ratio-test contribution.
-enum { ST_INVALID = 0, ST_VALID = 1, ST_AMBIG = 2 };
-struct Bracket {
-    int st;
-    float qh_dn, qh_up;  // bracket of (d > 0 ? ub - x : x - lb) / |d|   (upper step)
-    float ql_dn, ql_up;  // bracket of (d > 0 ? x - lb : ub - x) / |d|   (lower step magnitude)
+struct StepEntry {
+    double U;      // step uniform of attempt 0
+    double inv;    // 1 / (W + t + centre_offset)
+    unsigned idx;  // warmup index of attempt 0
+    unsigned pad;
 };
 
-// Decide, from FP32 approximations with error bounds, whether coordinate i is
-// certainly a ratio-test candidate (reference ACHRCuda.cu:270-279: distUb > dTol,
-// distLb > dTol and |u_i| > uTol), certainly not, or undecided; for certain
-// candidates bracket the two step ratios.
-__device__ __forceinline__ Bracket bracket(double x, double dk, float4 b, float dtol_hi, float dtol_lo,
-                                           float uthr_hi, float uthr_lo) {
-    Bracket c;
+// FP32 bracket of one coordinate's ratio-test contribution (reference
+// fillrandPoint, ACHRCuda.cu:266-281: a coordinate is a candidate when
+// distUb > dTol, distLb > dTol and |u_i| > uTol).  Writes the lower ends of
+// the two ratio brackets: NaN = certainly not a candidate, -inf = undecided
+// (evaluate in FP64), else the bracket's lower end; and folds the upper ends
+// of certain candidates into the running minima.
+__device__ __forceinline__ void bracket(double x, double dk, float2 b, float berr, float dtol_hi, float dtol_lo,
+                                        float uthr_hi, float uthr_lo, float &lo_h, float &lo_l, float &uh, float &ul,
+                                        int &fl) {
     const float x32 = f64_to_f32_rz(x);
     const float d32 = f64_to_f32_rz(dk);
     const float ad = fabsf(d32);
     const float Dp = b.y - x32;  // ub - x
     const float Dm = x32 - b.x;  // x - lb
-    const float ex = fmaf(fabsf(x32), kErrK, kTiny);
-    const float Ep = isinf(Dp) ? 0.0f : (b.w + ex) + fabsf(Dp) * kErrK;
-    const float Em = isinf(Dm) ? 0.0f : (b.z + ex) + fabsf(Dm) * kErrK;
+    const float ex = fmaf(fabsf(x32), kErrK, kTiny + berr);
+    const float Ep = fmaf(fabsf(Dp), kErrK, ex);
+    const float Em = fmaf(fabsf(Dm), kErrK, ex);
     const bool p_ok = (Dp - Ep) > dtol_hi, p_bad = (Dp + Ep) <= dtol_lo;
     const bool m_ok = (Dm - Em) > dtol_hi, m_bad = (Dm + Em) <= dtol_lo;
     const bool u_ok = ad > uthr_hi, u_bad = ad * kAdUp < uthr_lo;
-    c.st = (p_bad || m_bad || u_bad) ? ST_INVALID : ((p_ok && m_ok && u_ok) ? ST_VALID : ST_AMBIG);
-    const float r = __frcp_rn(ad);
+    const bool bad = p_bad || m_bad || u_bad;
+    const bool ok = p_ok && m_ok && u_ok;
+    const float r = rcp_approx(ad);
     const bool pos = d32 > 0.0f;
     const float nh = pos ? Dp : Dm, eh = pos ? Ep : Em;
     const float nl = pos ? Dm : Dp, el = pos ? Em : Ep;
-    c.qh_up = ((nh + eh) * r) * kUp;
-    c.qh_dn = ((nh - eh) * r) * kDn;
-    c.ql_up = ((nl + el) * r) * kUp;
-    c.ql_dn = ((nl - el) * r) * kDn;
-    return c;
-}
-
-// Exact FP64 candidate test and step ratios of one coordinate.
-__device__ __forceinline__ bool exact_candidate(double x, double dk, double lbv, double ubv, double dtol, double thr,
-                                            double &qh, double &ql) {
-    const double Dp = ubv - x, Dm = x - lbv;
-    if (!(Dp > dtol && Dm > dtol && fabs(dk) > thr)) return false;
-    const double ad = fabs(dk);
-    qh = (dk > 0.0 ? Dp : Dm) / ad;
-    ql = (dk > 0.0 ? Dm : Dp) / ad;
-    return true;
-}
-
-// Residual max|S x| with x in shared memory (reference findMaxAbs + the
-// serial max, ACHRCuda.cu:232-240, 326-337; here CSR rows, no atomics).
-__device__ __forceinline__ double residual_max(const ChainArgs &a, const double *xs, double *slot, int tid, int BD,
-                                               int lane, int warp, int nwarps) {
-    double mx = 0.0;
-    for (int row = tid; row < a.m; row += BD) {
-        double acc = 0.0;
-        const int q1 = __ldg(a.row_ptr + row + 1);
-        for (int q = __ldg(a.row_ptr + row); q < q1; ++q) acc = fma(__ldg(a.val + q), xs[__ldg(a.col_idx + q)], acc);
-        mx = fmax(mx, fabs(acc));
+    const float rup = r * kUp, rdn = r * kDn;
+    const float qh_up = (nh + eh) * rup, qh_dn = (nh - eh) * rdn;
+    const float ql_up = (nl + el) * rup, ql_dn = (nl - el) * rdn;
+    if (ok) {
+        uh = fminf(uh, qh_up);
+        ul = fminf(ul, ql_up);
     }
-    return block_max(mx, slot, lane, warp, nwarps);
-}
-
-// x <- N (N^T x) in FP64 (reference reprojectPoint / reprojectPoint2,
-// ACHRCuda.cu:208-230).  ys holds d doubles of shared scratch.
-__device__ __forceinline__ void reproject(const ChainArgs &a, double *xs, double *ys, int tid, int BD, int lane,
-                                          int warp, int nwarps) {
-    const int n = a.n;
-    for (int j = warp; j < a.d; j += nwarps) {
-        const double *Nj = a.N + (size_t)j * (size_t)n;
-        double acc = 0.0;
-        for (int i = lane; i < n; i += 32) acc = fma(__ldg(Nj + i), xs[i], acc);
-        acc = warp_sum(acc);
-        if (lane == 0) ys[j] = acc;
-    }
-    __syncthreads();
-    for (int i = tid; i < n; i += BD) {
-        double acc = 0.0;
-        for (int j = 0; j < a.d; ++j) acc = fma(__ldg(a.N + (size_t)j * (size_t)n + i), ys[j], acc);
-        xs[i] = acc;
-    }
-    __syncthreads();
-}
-
-__device__ __forceinline__ void atomic_max_nonneg(unsigned long long *slot, double v) {
-    if (v > 0.0) atomicMax(slot, (unsigned long long)__double_as_longlong(v));
+    lo_h = ok ? qh_dn : (bad ? __int_as_float(0x7fc00000) : -INFINITY);
+    lo_l = ok ? ql_dn : (bad ? __int_as_float(0x7fc00000) : -INFINITY);
+    fl |= ok ? 1 : 0;
+    fl |= (!ok && !bad) ? 2 : 0;
+    fl |= (!ok && !bad && !u_ok && !u_bad) ? 4 : 0;  // needs the FP64 norm
 }
 
 }  // namespace
 
-size_t chain_smem_bytes(int n, int d, int ldw, int block) {
-    (void)block;
-    const size_t npad = ((size_t)n + 15) & ~(size_t)15;
-    const size_t wpad = ((size_t)ldw + 15) & ~(size_t)15;
-    const size_t dpad = ((size_t)(d > 0 ? d : 1) + 15) & ~(size_t)15;
-    return sizeof(double) * (2 * npad + wpad + dpad) + sizeof(RedSlots) + 64;
+constexpr int kTbl = 64;  // steps per refill of the step table
+
+// Shared memory of one CTA: xs, As, ws (NP doubles each; ws doubles as the
+// reprojection scratch), the step table and the reduction slots.
+size_t chain_smem_bytes_cfg(int np, int d, int bd) {
+    (void)d;
+    (void)bd;
+    return sizeof(double) * 3 * (size_t)np + sizeof(StepEntry) * kTbl + 2 * sizeof(RedSlots) + 128;
 }
 
-template <int EPT>
-__global__ void __launch_bounds__(512, 1) achr_chain_kernel(const ChainArgs a) {
+template <int BD, int EPT>
+__global__ void __launch_bounds__(BD, (BD <= 256 ? 2 : 1)) achr_chain_kernel(const ChainArgs a) {
+    constexpr int NP = BD * EPT;
+    constexpr int NW = BD / 32;
     extern __shared__ __align__(128) unsigned char smem_raw[];
-    const int n = a.n;
-    const int BD = blockDim.x, tid = threadIdx.x;
-    const int lane = tid & 31, warp = tid >> 5, nwarps = BD >> 5;
-    const size_t npad = ((size_t)n + 15) & ~(size_t)15;
-    const size_t wpad = ((size_t)a.ldw + 15) & ~(size_t)15;
-    const size_t dpad = ((size_t)(a.d > 0 ? a.d : 1) + 15) & ~(size_t)15;
+    const int tid = threadIdx.x;
+    const int lane = tid & 31, warp = tid >> 5;
     double *xs = reinterpret_cast<double *>(smem_raw);
-    double *As = xs + npad;
-    double *ws = As + npad;
-    double *ys = ws + wpad;
-    RedSlots *rs = reinterpret_cast<RedSlots *>(ys + dpad);
-    uint64_t *bar = reinterpret_cast<uint64_t *>(rs + 1);
-    int *exact_count = reinterpret_cast<int *>(bar + 1);
+    double *As = xs + NP;
+    double *ws = As + NP;
+    double *ys = ws;  // reprojection scratch (d <= n entries, below the zero padding of ws)
+    StepEntry *tbl = reinterpret_cast<StepEntry *>(ws + NP);
+    RedSlots *rsb = reinterpret_cast<RedSlots *>(tbl + kTbl);
+    uint64_t *bar = reinterpret_cast<uint64_t *>(rsb + 2);
+    unsigned long long *cnt = reinterpret_cast<unsigned long long *>(bar + 1);  // CTA statistics, CNT_* slots
+    int *exact_count = reinterpret_cast<int *>(cnt + 8);
 
     if (tid == 0) {
         mbar_init(bar, 1);
         fence_mbar_init();
         *exact_count = 0;
+        for (int c = 0; c < 8; ++c) cnt[c] = 0;
     }
+    // The TMA copy fills ws[0, ldw); the padding beyond stays zero.
+#pragma unroll
+    for (int k = 0; k < EPT; ++k) ws[tid + k * BD] = 0.0;
     __syncthreads();
 
     const unsigned col_bytes = (unsigned)(sizeof(double) * (size_t)a.ldw);
-    const float dtol32 = (float)a.d_tol;
-    const float dtol_hi = dtol32 * kUp, dtol_lo = dtol32 * kDn;
-    unsigned phase = 0;
+    const float dtol_hi = a.dtol_hi, dtol_lo = a.dtol_lo, berr = a.bound_err;
+    const float utol32 = a.utol32, mmt32 = a.mmt32;
+    const unsigned long long res_tol_bits = (unsigned long long)__double_as_longlong(a.residual_tol);
+    unsigned phase = 0, it = 0;
     bool failed = false;
-    long long n_acc = 0, n_rej = 0, n_chk = 0, n_rep = 0, n_stuck = 0, n_fin = 0;
     double worst_res = 0.0, worst_viol = 0.0;
 
     for (long long p = blockIdx.x; p < a.P && !failed; p += gridDim.x) {
         const unsigned long long chain = a.chain_offset + (unsigned long long)p;
-        for (int i = tid; i < n; i += BD) {
+#pragma unroll
+        for (int k = 0; k < EPT; ++k) {
+            const int i = tid + k * BD;
             xs[i] = a.c0[i];
             As[i] = a.A0[i];
         }
         long long buf_col = -1;
         bool inflight = false, any_accepted = false, stuck = false;
-        __syncthreads();
+        int chk = 0;  // accepted steps since the last residual check (ACHRCuda.cu:325)
+        int tbase = -kTbl;
 
         for (int s = 0; s < a.T && !stuck && !failed; ++s) {
-            const double inv = 1.0 / (double)(a.W + s + a.centre_offset);
-            const Philox4 pd0 = step_draw(a.seed, chain, (uint32_t)s, 0u);
-            const double U = step_uniform(pd0);
-            for (int att = 0;; ++att) {
+            if (s - tbase >= kTbl) {
+                // refill the step table: entry e holds step tbase + e
+                tbase = s;
+                __syncthreads();
+                for (int e = tid; e < kTbl; e += BD) {
+                    const int st = s + e;
+                    if (st < a.T) {
+                        const Philox4 pd = step_draw(a.seed, chain, (uint32_t)st, 0u);
+                        StepEntry en;
+                        en.U = step_uniform(pd);
+                        en.inv = 1.0 / (double)(a.W + st + a.centre_offset);
+                        en.idx = warmup_index(pd, (uint32_t)a.W);
+                        en.pad = 0;
+                        tbl[e] = en;
+                    }
+                }
+                __syncthreads();
+            }
+            const StepEntry te = tbl[s - tbase];
+            const double ninv = -te.inv;
+            const double U = te.U;
+            for (int att = 0;; ++att, ++it) {
                 if (att >= a.max_attempts) {
                     stuck = true;
                     break;
                 }
-                const Philox4 pd = (att == 0) ? pd0 : step_draw(a.seed, chain, (uint32_t)s, (uint32_t)att);
-                const long long r = (long long)warmup_index(pd, (uint32_t)a.W);
-                __syncthreads();  // previous readers of ws and of the reduction slots are done
+                RedSlots *rs = rsb + (it & 1u);
+                const long long r = att == 0
+                                        ? (long long)te.idx
+                                        : (long long)warmup_index(step_draw(a.seed, chain, (uint32_t)s, (uint32_t)att),
+                                                                  (uint32_t)a.W);
                 if (buf_col != r) {
                     if (inflight) {
                         if (!mbar_wait_bounded(bar, phase)) failed = true;
                         phase ^= 1u;
                         inflight = false;
-                        __syncthreads();
+                    }
+                    __syncthreads();  // every thread has seen the previous phase complete
+                    if (r < 0 || r >= a.W) {  // never copy from outside the warmup matrix
+                        failed = true;
+                        break;
                     }
                     if (tid == 0) {
                         fence_proxy_async_smem();
@@ -339,30 +367,45 @@ __global__ void __launch_bounds__(512, 1) achr_chain_kernel(const ChainArgs a) {
                     phase ^= 1u;
                     inflight = false;
                 }
-                if (__syncthreads_or(failed ? 1 : 0)) {
-                    failed = true;
-                    break;
-                }
 
                 // Phase A: d = w_r - A / (W + t)  (reference ACHRCuda.cu:260-264)
                 double dreg[EPT];
-                double ss = 0.0;
+                float ss = 0.0f;
 #pragma unroll
                 for (int k = 0; k < EPT; ++k) {
                     const int i = tid + k * BD;
-                    double dk = 0.0;
-                    if (i < n) dk = fma(-As[i], inv, ws[i]);
+                    const double dk = fma(As[i], ninv, ws[i]);
                     dreg[k] = dk;
-                    ss = fma(dk, dk, ss);
+                    const float d32 = f64_to_f32_rz(dk);
+                    ss = fmaf(d32, d32, ss);
                 }
-                ss = block_sum(ss, rs->sum, lane, warp, nwarps);
-                const double norm = sqrt(ss);
+#pragma unroll
+                for (int o = 16; o; o >>= 1) ss += __shfl_xor_sync(0xffffffffu, ss, o);
+                if (lane == 0) {
+                    rs->sum1[warp] = ss;
+                    rs->flag1[warp] = failed ? 1 : 0;
+                }
+                __syncthreads();
+                ss = 0.0f;
+                int f1 = 0;
+#pragma unroll
+                for (int w = 0; w < NW; ++w) {
+                    ss += rs->sum1[w];
+                    f1 |= rs->flag1[w];
+                }
+                if (f1) {
+                    failed = true;
+                    break;
+                }
+                const float norm32 = sqrtf(ss);
 
                 // Prefetch the next step's warmup column while this one is tested.
                 if (s + 1 < a.T) {
                     const long long rn =
-                        (long long)warmup_index(step_draw(a.seed, chain, (uint32_t)(s + 1), 0u), (uint32_t)a.W);
-                    if (rn != buf_col) {
+                        (s + 1 - tbase < kTbl)
+                            ? (long long)tbl[s + 1 - tbase].idx
+                            : (long long)warmup_index(step_draw(a.seed, chain, (uint32_t)(s + 1), 0u), (uint32_t)a.W);
+                    if (rn != buf_col && rn >= 0 && rn < a.W) {
                         if (tid == 0) {
                             fence_proxy_async_smem();
                             mbar_arrive_expect_tx(bar, col_bytes);
@@ -372,103 +415,184 @@ __global__ void __launch_bounds__(512, 1) achr_chain_kernel(const ChainArgs a) {
                         buf_col = rn;
                     }
                 }
-                if (!(norm > 0.0) || !isfinite(norm)) {
-                    ++n_rej;
+                if (!(norm32 > 0.0f) || !(norm32 < INFINITY)) {
+                    if (tid == 0) ++cnt[CNT_REJECTED];
                     continue;
                 }
 
                 // Phase B1: FP32 brackets (reference ratio test ACHRCuda.cu:266-281)
-                const double thr = a.u_tol * norm;
-                const float uthr = (float)thr;
-                const float uthr_hi = uthr * kUp, uthr_lo = uthr * kDn;
+                const float uthr = utol32 * norm32;
+                const float uthr_hi = uthr * kNormUp, uthr_lo = uthr * kNormDn;
                 float uh = INFINITY, ul = INFINITY;
-                int fl = a.exact_ratio ? 2 : 0;
+                float my_lh = INFINITY, my_ll = INFINITY;  // this thread's smallest bracket lower ends
+                int fl = 0;
                 if (!a.exact_ratio) {
 #pragma unroll
                     for (int k = 0; k < EPT; ++k) {
                         const int i = tid + k * BD;
-                        if (i < n) {
-                            const Bracket c = bracket(xs[i], dreg[k], __ldg(a.bnd32 + i), dtol_hi, dtol_lo, uthr_hi,
-                                                      uthr_lo);
-                            if (c.st == ST_VALID) {
-                                uh = fminf(uh, c.qh_up);
-                                ul = fminf(ul, c.ql_up);
-                                fl |= 1;
-                            } else if (c.st == ST_AMBIG) {
-                                fl |= 2;
-                            }
-                        }
+                        float lo_h, lo_l;
+                        bracket(xs[i], dreg[k], __ldg(a.bnd + i), berr, dtol_hi, dtol_lo, uthr_hi, uthr_lo, lo_h, lo_l,
+                                uh, ul, fl);
+                        my_lh = fminf(my_lh, lo_h);  // NaN (not a candidate) is ignored, -inf (undecided) wins
+                        my_ll = fminf(my_ll, lo_l);
                     }
+                } else {
+                    fl = 2 | 4;
+                    my_lh = my_ll = -INFINITY;
                 }
-                uh = warp_minf(uh);
-                ul = warp_minf(ul);
-                fl = warp_or(fl);
+#pragma unroll
+                for (int o = 16; o; o >>= 1) {
+                    uh = fminf(uh, __shfl_xor_sync(0xffffffffu, uh, o));
+                    ul = fminf(ul, __shfl_xor_sync(0xffffffffu, ul, o));
+                    fl |= __shfl_xor_sync(0xffffffffu, fl, o);
+                }
                 if (lane == 0) {
-                    rs->fmin2[warp] = make_float2(uh, ul);
+                    rs->min2[warp] = make_float2(uh, ul);
                     rs->flag2[warp] = fl;
                 }
                 __syncthreads();
                 uh = INFINITY;
                 ul = INFINITY;
                 fl = 0;
-                for (int w = 0; w < nwarps; ++w) {
-                    const float2 v = rs->fmin2[w];
+#pragma unroll
+                for (int w = 0; w < NW; ++w) {
+                    const float2 v = rs->min2[w];
                     uh = fminf(uh, v.x);
                     ul = fminf(ul, v.y);
                     fl |= rs->flag2[w];
                 }
 
+                // FP64 norm, only when some candidacy test sits inside the FP32
+                // norm's margin (or every candidate is evaluated in FP64).
+                double thr64 = 0.0;
+                bool have_norm64 = false;
+                double norm64 = 0.0;
+                if (fl & 4) {
+                    double s64 = 0.0;
+#pragma unroll
+                    for (int k = 0; k < EPT; ++k) s64 = fma(dreg[k], dreg[k], s64);
+#pragma unroll
+                    for (int o = 16; o; o >>= 1) s64 += __shfl_xor_sync(0xffffffffu, s64, o);
+                    if (lane == 0) rs->sum5[warp] = s64;
+                    __syncthreads();
+                    s64 = 0.0;
+#pragma unroll
+                    for (int w = 0; w < NW; ++w) s64 += rs->sum5[w];
+                    norm64 = sqrt(s64);
+                    have_norm64 = true;
+                    thr64 = a.u_tol * norm64;
+                }
+
                 // Phase B2: FP64 evaluation of every coordinate whose bracket can
                 // hold a minimum, or whose candidacy the brackets left open.
-                double qh = INFINITY, ql = INFINITY;
+                unsigned long long kh = kInfBits, kl = kInfBits;
                 int anyv = 0, nex = 0;
+                unsigned mh = 0, ml = 0, mam = 0;  // bit k: contender for max / min step, undecided
+                // Only a thread whose own bracket lower ends reach the block minima
+                // can hold a contender; the others skip the second pass.
+                const bool mine = my_lh <= uh || my_ll <= ul;
+                if (!a.exact_ratio && mine) {
 #pragma unroll
-                for (int k = 0; k < EPT; ++k) {
+                    for (int k = 0; k < EPT; ++k) {
+                        const int i = tid + k * BD;
+                        float lo_h, lo_l, uh2 = INFINITY, ul2 = INFINITY;  // minima already known
+                        int fl2 = 0;
+                        bracket(xs[i], dreg[k], __ldg(a.bnd + i), berr, dtol_hi, dtol_lo, uthr_hi, uthr_lo, lo_h, lo_l,
+                                uh2, ul2, fl2);
+                        mh |= (lo_h <= uh ? 1u : 0u) << k;
+                        ml |= (lo_l <= ul ? 1u : 0u) << k;
+                        mam |= (lo_h == -INFINITY ? 1u : 0u) << k;
+                    }
+                } else if (a.exact_ratio) {
+                    mh = ml = mam = (EPT >= 32) ? 0xFFFFFFFFu : ((1u << EPT) - 1u);
+                }
+                for (unsigned m = mh | ml; m; m &= m - 1) {
+                    const int k = __ffs(m) - 1;
+                    const unsigned bit = 1u << k;
                     const int i = tid + k * BD;
-                    if (i < n) {
-                        const double xi = xs[i];
-                        bool contender = a.exact_ratio != 0;
-                        if (!contender) {
-                            const Bracket c =
-                                bracket(xi, dreg[k], __ldg(a.bnd32 + i), dtol_hi, dtol_lo, uthr_hi, uthr_lo);
-                            contender = (c.st == ST_AMBIG) ||
-                                        (c.st == ST_VALID && (c.qh_dn <= uh || c.ql_dn <= ul));
+                    ++nex;
+                    const double xi = xs[i], dk = pick(dreg, k);
+                    const double2 lu = ld_lbub(a.lbub + i);
+                    const double Dp = lu.y - xi, Dm = xi - lu.x;
+                    bool valid = true;
+                    if (mam & bit) {  // undecided: full FP64 candidacy test
+                        bool u_pass;
+                        if (have_norm64) {
+                            u_pass = abs_bits(dk) > (unsigned long long)__double_as_longlong(thr64);
+                        } else {
+                            u_pass = fabsf(f64_to_f32_rz(dk)) > uthr_hi;
                         }
-                        if (contender) {
-                            ++nex;
-                            double eh, el;
-                            if (exact_candidate(xi, dreg[k], __ldg(a.lb + i), __ldg(a.ub + i), a.d_tol, thr, eh, el)) {
-                                qh = fmin(qh, eh);
-                                ql = fmin(ql, el);
-                                anyv = 1;
-                            }
-                        }
+                        valid = Dp > a.d_tol && Dm > a.d_tol && u_pass;
+                    }
+                    if (valid) {
+                        const double ad = abs_int(dk);
+                        const bool pos = positive_int(dk);
+                        if (mh & bit) kh = umin(kh, (unsigned long long)__double_as_longlong((pos ? Dp : Dm) / ad));
+                        if (ml & bit) kl = umin(kl, (unsigned long long)__double_as_longlong((pos ? Dm : Dp) / ad));
+                        anyv = 1;
                     }
                 }
                 if (nex) atomicAdd(exact_count, nex);
-                qh = warp_min(qh);
-                ql = warp_min(ql);
-                anyv = warp_or(anyv);
+#pragma unroll
+                for (int o = 16; o; o >>= 1) {
+                    kh = umin(kh, shfl_u64(kh, o));
+                    kl = umin(kl, shfl_u64(kl, o));
+                    anyv |= __shfl_xor_sync(0xffffffffu, anyv, o);
+                }
                 if (lane == 0) {
-                    rs->dmin2[warp] = make_double2(qh, ql);
+                    rs->min3[warp] = make_ulonglong2(kh, kl);
                     rs->flag3[warp] = anyv;
                 }
                 __syncthreads();
-                qh = INFINITY;
-                ql = INFINITY;
+                kh = kInfBits;
+                kl = kInfBits;
                 anyv = 0;
-                for (int w = 0; w < nwarps; ++w) {
-                    const double2 v = rs->dmin2[w];
-                    qh = fmin(qh, v.x);
-                    ql = fmin(ql, v.y);
+#pragma unroll
+                for (int w = 0; w < NW; ++w) {
+                    const ulonglong2 v = rs->min3[w];
+                    kh = umin(kh, v.x);
+                    kl = umin(kl, v.y);
                     anyv |= rs->flag3[w];
                 }
+                if (!anyv) {  // no candidate: rejection (see ACHRCuda.cu:283-288)
+                    if (tid == 0) ++cnt[CNT_REJECTED];
+                    continue;
+                }
+                const double qh = __longlong_as_double((long long)kh);
+                const double ql = __longlong_as_double((long long)kl);
 
-                // Rejection test (reference ACHRCuda.cu:316-319; no candidate = rejection)
-                const double maxStep = qh * norm, minStep = -(ql * norm);
-                if (!anyv || (fabs(minStep) < a.max_min_tol && fabs(maxStep) < a.max_min_tol) ||
-                    minStep > maxStep) {
-                    ++n_rej;
+                // Rejection test |min| < tol && |max| < tol (ACHRCuda.cu:316-319),
+                // min = -ql ||d||, max = qh ||d||; FP32 unless inside the margin.
+                bool reject;
+                {
+                    const float qh32 = f64_to_f32_rz(qh), ql32 = f64_to_f32_rz(ql);
+                    const float th_lo = qh32 * norm32 * kNormDn, th_hi = qh32 * kAdUp * norm32 * kNormUp;
+                    const float tl_lo = ql32 * norm32 * kNormDn, tl_hi = ql32 * kAdUp * norm32 * kNormUp;
+                    const float tol_lo = mmt32 * kDn, tol_hi = mmt32 * kUp;
+                    const bool big = th_lo >= tol_hi || tl_lo >= tol_hi;
+                    const bool small = th_hi < tol_lo && tl_hi < tol_lo;
+                    if (big) {
+                        reject = false;
+                    } else if (small) {
+                        reject = true;
+                    } else {
+                        double s64 = 0.0;
+#pragma unroll
+                        for (int k = 0; k < EPT; ++k) s64 = fma(dreg[k], dreg[k], s64);
+#pragma unroll
+                        for (int o = 16; o; o >>= 1) s64 += __shfl_xor_sync(0xffffffffu, s64, o);
+                        __syncthreads();  // slot sum5 may hold this attempt's earlier norm
+                        if (lane == 0) rs->sum5[warp] = s64;
+                        __syncthreads();
+                        s64 = 0.0;
+#pragma unroll
+                        for (int w = 0; w < NW; ++w) s64 += rs->sum5[w];
+                        const double nrm = sqrt(s64);
+                        reject = fabs(ql * nrm) < a.max_min_tol && fabs(qh * nrm) < a.max_min_tol;
+                    }
+                }
+                if (reject) {
+                    if (tid == 0) ++cnt[CNT_REJECTED];
                     continue;
                 }
                 // t / ||d|| with t = U (max - min) + min (reference ACHRCuda.cu:314)
@@ -476,42 +600,99 @@ __global__ void __launch_bounds__(512, 1) achr_chain_kernel(const ChainArgs a) {
 
                 // Phase C: x = prev + t u (ACHRCuda.cu:242-249), residual check every
                 // check_period steps (:325-344), clip + centre (:193-206, :347-350).
-                const bool check = (s % a.check_period) == 0;
+                const bool check = chk == 0;
+                chk = (chk + 1 == a.check_period) ? 0 : chk + 1;
                 if (!check) {
+                    unsigned edge = 0;  // bit k: not provably inside the box, clip exactly below
 #pragma unroll
                     for (int k = 0; k < EPT; ++k) {
                         const int i = tid + k * BD;
-                        if (i < n) {
-                            const double xn = fma(sstep, dreg[k], xs[i]);
-                            const double xc = fmin(fmax(xn, __ldg(a.lb + i)), __ldg(a.ub + i));
-                            xs[i] = xc;
-                            As[i] += xc;
-                        }
+                        const double xn = fma(sstep, dreg[k], xs[i]);
+                        xs[i] = xn;
+                        if (surely_inside(f64_to_f32_rz(xn), __ldg(a.bnd + i), berr)) As[i] += xn;
+                        else edge |= 1u << k;
+                    }
+                    for (; edge; edge &= edge - 1) {
+                        const int i = tid + (__ffs(edge) - 1) * BD;
+                        const double xc = clip_exact(xs[i], ld_lbub(a.lbub + i));
+                        xs[i] = xc;
+                        As[i] += xc;
                     }
                 } else {
 #pragma unroll
                     for (int k = 0; k < EPT; ++k) {
                         const int i = tid + k * BD;
-                        if (i < n) xs[i] = fma(sstep, dreg[k], xs[i]);
+                        xs[i] = fma(sstep, dreg[k], xs[i]);
                     }
                     __syncthreads();
-                    ++n_chk;
-                    const double mx = residual_max(a, xs, rs->mx, tid, BD, lane, warp, nwarps);
-                    if (mx > a.residual_tol) {
-                        ++n_rep;
-                        reproject(a, xs, ys, tid, BD, lane, warp, nwarps);
+                    if (tid == 0) ++cnt[CNT_CHECKS];
+                    unsigned long long mx = 0;
+                    for (int row = tid; row < a.m; row += BD) {
+                        double acc = 0.0;
+                        const int q1 = __ldg(a.row_ptr + row + 1);
+                        for (int q = __ldg(a.row_ptr + row); q < q1; ++q)
+                            acc = fma(__ldg(a.val + q), xs[__ldg(a.col_idx + q)], acc);
+                        mx = umax(mx, abs_bits(acc));
                     }
+#pragma unroll
+                    for (int o = 16; o; o >>= 1) mx = umax(mx, shfl_u64(mx, o));
+                    if (lane == 0) rs->max4[warp] = mx;
+                    __syncthreads();
+                    mx = 0;
+#pragma unroll
+                    for (int w = 0; w < NW; ++w) mx = umax(mx, rs->max4[w]);
+                    if (mx > res_tol_bits) {
+                        // x <- N (N^T x) in FP64 (reference reprojectPoint(2), ACHRCuda.cu:208-230).
+                        // The scratch is ws: let the prefetched column land, use the
+                        // buffer, then fetch the column again.
+                        if (tid == 0) ++cnt[CNT_REPROJ];
+                        if (inflight) {
+                            if (!mbar_wait_bounded(bar, phase)) failed = true;
+                            phase ^= 1u;
+                            inflight = false;
+                        }
+                        __syncthreads();
+                        const int n = a.n;
+                        for (int j = warp; j < a.d; j += NW) {
+                            const double *Nj = a.N + (size_t)j * (size_t)n;
+                            double acc = 0.0;
+                            for (int i = lane; i < n; i += 32) acc = fma(__ldg(Nj + i), xs[i], acc);
+#pragma unroll
+                            for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+                            if (lane == 0) ys[j] = acc;
+                        }
+                        __syncthreads();
+                        for (int i = tid; i < n; i += BD) {
+                            double acc = 0.0;
+                            for (int j = 0; j < a.d; ++j) acc = fma(__ldg(a.N + (size_t)j * (size_t)n + i), ys[j], acc);
+                            xs[i] = acc;
+                        }
+                        __syncthreads();
+                        if (buf_col >= 0) {
+                            if (tid == 0) {
+                                fence_proxy_async_smem();
+                                mbar_arrive_expect_tx(bar, col_bytes);
+                                tma_load_1d(ws, a.warmup + (size_t)buf_col * (size_t)a.ldw, col_bytes, bar);
+                            }
+                            inflight = true;
+                        }
+                    }
+                    unsigned edge = 0;
 #pragma unroll
                     for (int k = 0; k < EPT; ++k) {
                         const int i = tid + k * BD;
-                        if (i < n) {
-                            const double xc = fmin(fmax(xs[i], __ldg(a.lb + i)), __ldg(a.ub + i));
-                            xs[i] = xc;
-                            As[i] += xc;
-                        }
+                        const double xv = xs[i];
+                        if (surely_inside(f64_to_f32_rz(xv), __ldg(a.bnd + i), berr)) As[i] += xv;
+                        else edge |= 1u << k;
+                    }
+                    for (; edge; edge &= edge - 1) {
+                        const int i = tid + (__ffs(edge) - 1) * BD;
+                        const double xc = clip_exact(xs[i], ld_lbub(a.lbub + i));
+                        xs[i] = xc;
+                        As[i] += xc;
                     }
                 }
-                ++n_acc;
+                if (tid == 0) ++cnt[CNT_ACCEPTED];
                 any_accepted = true;
                 break;
             }
@@ -521,8 +702,7 @@ __global__ void __launch_bounds__(512, 1) achr_chain_kernel(const ChainArgs a) {
             phase ^= 1u;
             inflight = false;
         }
-        if (stuck) ++n_stuck;
-        __syncthreads();
+        if (stuck && tid == 0) ++cnt[CNT_STUCK];
         if (__syncthreads_or(failed ? 1 : 0)) {
             failed = true;
             break;
@@ -531,70 +711,111 @@ __global__ void __launch_bounds__(512, 1) achr_chain_kernel(const ChainArgs a) {
         // Emitted point: residual / bound diagnostics and, on request, the final
         // feasibility projection (project, clip, re-check).
         if (any_accepted) {
-            double res = residual_max(a, xs, rs->mx, tid, BD, lane, warp, nwarps);
-            if (a.final_project && res > a.feasibility_tol) {
-                ++n_fin;
+            RedSlots *rs = rsb;
+            const int n = a.n;
+            unsigned long long res = 0;
+            for (int pass = 0; pass < 2; ++pass) {
+                unsigned long long mx = 0;
+                for (int row = tid; row < a.m; row += BD) {
+                    double acc = 0.0;
+                    const int q1 = __ldg(a.row_ptr + row + 1);
+                    for (int q = __ldg(a.row_ptr + row); q < q1; ++q)
+                        acc = fma(__ldg(a.val + q), xs[__ldg(a.col_idx + q)], acc);
+                    mx = umax(mx, abs_bits(acc));
+                }
+#pragma unroll
+                for (int o = 16; o; o >>= 1) mx = umax(mx, shfl_u64(mx, o));
                 __syncthreads();
-                reproject(a, xs, ys, tid, BD, lane, warp, nwarps);
-                for (int i = tid; i < n; i += BD) xs[i] = fmin(fmax(xs[i], __ldg(a.lb + i)), __ldg(a.ub + i));
+                if (lane == 0) rs->max4[warp] = mx;
                 __syncthreads();
-                res = residual_max(a, xs, rs->viol, tid, BD, lane, warp, nwarps);
+                res = 0;
+#pragma unroll
+                for (int w = 0; w < NW; ++w) res = umax(res, rs->max4[w]);
+                if (pass == 1 || !a.final_project || __longlong_as_double((long long)res) <= a.feasibility_tol) break;
+                if (tid == 0) ++cnt[CNT_FINAL_PROJ];
+                for (int j = warp; j < a.d; j += NW) {
+                    const double *Nj = a.N + (size_t)j * (size_t)n;
+                    double acc = 0.0;
+                    for (int i = lane; i < n; i += 32) acc = fma(__ldg(Nj + i), xs[i], acc);
+#pragma unroll
+                    for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+                    if (lane == 0) ys[j] = acc;
+                }
+                __syncthreads();
+                for (int i = tid; i < n; i += BD) {
+                    double acc = 0.0;
+                    for (int j = 0; j < a.d; ++j) acc = fma(__ldg(a.N + (size_t)j * (size_t)n + i), ys[j], acc);
+                    xs[i] = clip_exact(acc, ld_lbub(a.lbub + i));
+                }
+                __syncthreads();
             }
             double viol = 0.0;
             for (int i = tid; i < n; i += BD) {
                 const double xi = xs[i];
-                viol = fmax(viol, fmax(__ldg(a.lb + i) - xi, xi - __ldg(a.ub + i)));
+                const double2 lu = ld_lbub(a.lbub + i);
+                viol = fmax(viol, fmax(lu.x - xi, xi - lu.y));
             }
+            unsigned long long vb = (unsigned long long)__double_as_longlong(viol);
+#pragma unroll
+            for (int o = 16; o; o >>= 1) vb = umax(vb, shfl_u64(vb, o));
             __syncthreads();
-            viol = block_max(viol, rs->viol, lane, warp, nwarps);
-            worst_res = fmax(worst_res, res);
-            worst_viol = fmax(worst_viol, viol);
+            if (lane == 0) rs->max4[warp] = vb;
+            __syncthreads();
+            vb = 0;
+#pragma unroll
+            for (int w = 0; w < NW; ++w) vb = umax(vb, rs->max4[w]);
+            worst_res = fmax(worst_res, __longlong_as_double((long long)res));
+            worst_viol = fmax(worst_viol, __longlong_as_double((long long)vb));
         }
-        for (int i = tid; i < n; i += BD) a.out[(size_t)i * (size_t)a.ld_out + (size_t)p] = any_accepted ? xs[i] : 0.0;
+        for (int i = tid; i < a.n; i += BD) a.out[(size_t)i * (size_t)a.ld_out + (size_t)p] = any_accepted ? xs[i] : 0.0;
         __syncthreads();
     }
 
     __syncthreads();
     if (tid == 0) {
         unsigned long long *c = a.counters;
-        if (n_acc) atomicAdd(c + CNT_ACCEPTED, (unsigned long long)n_acc);
-        if (n_rej) atomicAdd(c + CNT_REJECTED, (unsigned long long)n_rej);
-        if (n_chk) atomicAdd(c + CNT_CHECKS, (unsigned long long)n_chk);
-        if (n_rep) atomicAdd(c + CNT_REPROJ, (unsigned long long)n_rep);
-        if (n_stuck) atomicAdd(c + CNT_STUCK, (unsigned long long)n_stuck);
-        if (n_fin) atomicAdd(c + CNT_FINAL_PROJ, (unsigned long long)n_fin);
+        const int slots[6] = {CNT_ACCEPTED, CNT_REJECTED, CNT_CHECKS, CNT_REPROJ, CNT_STUCK, CNT_FINAL_PROJ};
+        for (int q = 0; q < 6; ++q)
+            if (cnt[slots[q]]) atomicAdd(c + slots[q], cnt[slots[q]]);
         if (*exact_count) atomicAdd(c + CNT_EXACT, (unsigned long long)*exact_count);
-        atomic_max_nonneg(c + CNT_MAXRES_BITS, worst_res);
-        atomic_max_nonneg(c + CNT_MAXVIOL_BITS, worst_viol);
+        if (worst_res > 0.0) atomicMax(c + CNT_MAXRES_BITS, (unsigned long long)__double_as_longlong(worst_res));
+        if (worst_viol > 0.0) atomicMax(c + CNT_MAXVIOL_BITS, (unsigned long long)__double_as_longlong(worst_viol));
         if (failed) atomicOr(c + CNT_ERROR, ERR_TMA_TIMEOUT);
     }
 }
 
-int chain_block_size(int n, int threads_per_chain) {
-    if (threads_per_chain > 0) return threads_per_chain;
-    int bd = 32 * ((n + 32 * 16 - 1) / (32 * 16));
-    if (bd < 32) bd = 32;
-    if (bd > 512) bd = 512;
-    return bd;
-}
+// Block size / elements-per-thread ladder: the smallest padded length BD*EPT >= n.
+struct Cfg {
+    int bd, ept;
+};
+static const Cfg kLadder[] = {{32, 4}, {64, 4}, {128, 4}, {128, 8}, {256, 8}, {256, 16}, {512, 16}, {512, 32}};
 
-static int pick_ept(int n, int bd) {
-    const int need = (n + bd - 1) / bd;
-    if (need <= 1) return 1;
-    if (need <= 2) return 2;
-    if (need <= 4) return 4;
-    if (need <= 8) return 8;
-    if (need <= 16) return 16;
-    if (need <= 32) return 32;
+int chain_padded_length(int n, int threads_per_chain) {
+    for (const Cfg &c : kLadder)
+        if ((threads_per_chain == 0 || c.bd == threads_per_chain) && c.bd * c.ept >= n) return c.bd * c.ept;
     return 0;
 }
 
-template <int EPT>
-static cudaError_t launch_ept(const ChainArgs &a, int bd, size_t smem, cudaStream_t stream) {
-    cudaError_t e = cudaFuncSetAttribute(achr_chain_kernel<EPT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+int chain_block_size(int n, int threads_per_chain) {
+    for (const Cfg &c : kLadder)
+        if ((threads_per_chain == 0 || c.bd == threads_per_chain) && c.bd * c.ept >= n) return c.bd;
+    return 0;
+}
+
+size_t chain_smem_bytes(int n, int d, int ldw, int block) {
+    (void)ldw;
+    const int np = chain_padded_length(n, block);
+    return chain_smem_bytes_cfg(np, d, block);
+}
+
+template <int BD, int EPT>
+static cudaError_t launch_cfg(const ChainArgs &a, cudaStream_t stream) {
+    const size_t smem = chain_smem_bytes_cfg(BD * EPT, a.d, BD);
+    cudaError_t e = cudaFuncSetAttribute(achr_chain_kernel<BD, EPT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
     if (e != cudaSuccess) return e;
     int per_sm = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, achr_chain_kernel<EPT>, bd, smem);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, achr_chain_kernel<BD, EPT>, BD, smem);
     if (e != cudaSuccess) return e;
     if (per_sm < 1) return cudaErrorInvalidConfiguration;
     int dev = 0, sms = 0;
@@ -603,23 +824,24 @@ static cudaError_t launch_ept(const ChainArgs &a, int bd, size_t smem, cudaStrea
     long long grid = (long long)sms * per_sm;
     if (grid > a.P) grid = a.P;
     if (grid < 1) return cudaSuccess;
-    achr_chain_kernel<EPT><<<(unsigned)grid, bd, smem, stream>>>(a);
+    achr_chain_kernel<BD, EPT><<<(unsigned)grid, BD, smem, stream>>>(a);
     return cudaGetLastError();
 }
 
 cudaError_t launch_chains(const ChainArgs &a, int threads_per_chain, cudaStream_t stream) {
     if (a.P <= 0) return cudaSuccess;
     const int bd = chain_block_size(a.n, threads_per_chain);
-    if (bd % 32 != 0 || bd < 32 || bd > 512) return cudaErrorInvalidValue;
-    const int ept = pick_ept(a.n, bd);
-    const size_t smem = chain_smem_bytes(a.n, a.d, a.ldw, bd);
-    switch (ept) {
-        case 1: return launch_ept<1>(a, bd, smem, stream);
-        case 2: return launch_ept<2>(a, bd, smem, stream);
-        case 4: return launch_ept<4>(a, bd, smem, stream);
-        case 8: return launch_ept<8>(a, bd, smem, stream);
-        case 16: return launch_ept<16>(a, bd, smem, stream);
-        case 32: return launch_ept<32>(a, bd, smem, stream);
+    const int np = chain_padded_length(a.n, threads_per_chain);
+    if (bd == 0 || np != a.np) return cudaErrorInvalidValue;
+    switch (np / bd * 10000 + bd) {
+        case 4 * 10000 + 32: return launch_cfg<32, 4>(a, stream);
+        case 4 * 10000 + 64: return launch_cfg<64, 4>(a, stream);
+        case 4 * 10000 + 128: return launch_cfg<128, 4>(a, stream);
+        case 8 * 10000 + 128: return launch_cfg<128, 8>(a, stream);
+        case 8 * 10000 + 256: return launch_cfg<256, 8>(a, stream);
+        case 16 * 10000 + 256: return launch_cfg<256, 16>(a, stream);
+        case 16 * 10000 + 512: return launch_cfg<512, 16>(a, stream);
+        case 32 * 10000 + 512: return launch_cfg<512, 32>(a, stream);
         default: return cudaErrorInvalidValue;
     }
 }

@@ -27,13 +27,17 @@ enum DeviceError : unsigned long long {
 // Everything one chain-sampling launch reads (device pointers) and its scalars.
 struct ChainArgs {
     int n, m, W, d;
+    int np;                     // padded length of the per-element arrays (block size x elements per thread)
     int ldw;                    // leading dimension of the warmup matrix in doubles (even)
     int P, T;
     const double *warmup;       // ldw x W, column j = warmup point j
-    const double *c0;           // n: start point and initial centre
-    const double *A0;           // n: (W + centre_offset) * c0, the centre accumulator at step 0
-    const double *lb, *ub;      // n
-    const float4 *bnd32;        // n: (float lb, float ub, |lb - float lb|, |ub - float ub|), errors rounded up
+    const double *c0;           // np: start point and initial centre (zero padding)
+    const double *A0;           // np: (W + centre_offset) * c0, the centre accumulator at step 0
+    const double2 *lbub;        // np: (lb, ub) in FP64; padding (0, 0)
+    const float2 *bnd;          // np: (lb, ub) rounded to FP32, infinite bounds as -+3e38; padding (-1, 1)
+    float bound_err;            // max |lb - float(lb)|, |ub - float(ub)| over finite bounds, rounded up
+    float dtol_hi, dtol_lo;     // FP32 brackets of d_tol (1 +- 2^-20)
+    float utol32, mmt32;        // u_tol and max_min_tol in FP32
     const int *row_ptr;         // CSR of S (m + 1)
     const int *col_idx;
     const double *val;
@@ -50,8 +54,10 @@ struct ChainArgs {
 // Launch the persistent chain kernel; threads_per_chain = 0 picks by size.
 cudaError_t launch_chains(const ChainArgs &a, int threads_per_chain, cudaStream_t stream);
 
-// Shared-memory bytes and block size the launcher would use (for tests/tuning).
+// Block size and padded element count the launcher uses for n reactions
+// (threads_per_chain = 0 picks by size); 0 if no configuration fits.
 int chain_block_size(int n, int threads_per_chain);
+int chain_padded_length(int n, int threads_per_chain);
 size_t chain_smem_bytes(int n, int d, int ldw, int block);
 
 }  // namespace achr
