@@ -390,9 +390,31 @@ achr_status achr_create(const achr_model *model, const double *warmup, int32_t n
 
     ACHR_CUDA_TRY(ctx->lbub.upload(lu.data(), np));
     ACHR_CUDA_TRY(ctx->bnd.upload(b32.data(), np));
-    ACHR_CUDA_TRY(ctx->rowptr.upload(ctx->h_rowptr.data(), ctx->h_rowptr.size()));
-    ACHR_CUDA_TRY(ctx->colidx.upload(ctx->h_colidx.data(), ctx->h_colidx.size()));
-    ACHR_CUDA_TRY(ctx->val.upload(ctx->h_val.data(), ctx->h_val.size()));
+    {
+        // The device copy of S lists rows longest first, so the 32 rows a warp
+        // sums together in the residual check have similar lengths; max|S x|
+        // does not depend on the row order.
+        std::vector<int> order_r((size_t)m);
+        for (int r = 0; r < m; ++r) order_r[(size_t)r] = r;
+        std::stable_sort(order_r.begin(), order_r.end(), [&](int a, int b) {
+            return ctx->h_rowptr[(size_t)a + 1] - ctx->h_rowptr[a] > ctx->h_rowptr[(size_t)b + 1] - ctx->h_rowptr[b];
+        });
+        std::vector<int> rp((size_t)m + 1, 0), ci;
+        std::vector<double> vv;
+        ci.reserve(ctx->h_colidx.size());
+        vv.reserve(ctx->h_val.size());
+        for (int q = 0; q < m; ++q) {
+            const int r = order_r[(size_t)q];
+            for (int t = ctx->h_rowptr[r]; t < ctx->h_rowptr[(size_t)r + 1]; ++t) {
+                ci.push_back(ctx->h_colidx[t]);
+                vv.push_back(ctx->h_val[t]);
+            }
+            rp[(size_t)q + 1] = (int)ci.size();
+        }
+        ACHR_CUDA_TRY(ctx->rowptr.upload(rp.data(), rp.size()));
+        ACHR_CUDA_TRY(ctx->colidx.upload(ci.data(), ci.size()));
+        ACHR_CUDA_TRY(ctx->val.upload(vv.data(), vv.size()));
+    }
     ACHR_CUDA_TRY(ctx->counters.alloc(achr::CNT_SLOTS));
 
     // Warmup matrix with an even leading dimension so every column starts on a

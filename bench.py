@@ -139,14 +139,15 @@ class ClockSampler:
 def cpu_baseline(oracle, model, warm, N, T, seed, target_s):
     """Time the oracle (all host threads) on a bounded chain sample of the workload."""
     threads = os.cpu_count() or 1
-    probe_chains, probe_steps = threads, 20
+    prob = oracle.Problem(model, warm, N)
+    probe_steps = 50
     t0 = time.perf_counter()
-    oracle.sample(model, warm, N, seed, probe_chains, probe_steps, chain_offset=10**9, threads=threads)
+    prob.sample(seed, threads, probe_steps, chain_offset=10**9, threads=threads)
     per_round = (time.perf_counter() - t0) / probe_steps  # seconds per step for `threads` chains
     rounds = max(1, int(target_s / max(per_round * T, 1e-9)))
     P = threads * rounds
     t0 = time.perf_counter()
-    _, st = oracle.sample(model, warm, N, seed, P, T, threads=threads)
+    _, st = prob.sample(seed, P, T, threads=threads)
     el = time.perf_counter() - t0
     return {"value": st["accepted"] / el, "unit": METRIC, "cores": threads, "kind": "port",
             "sample": f"{P} chains x {T} steps of the same workload ({st['accepted']} chain-steps, {el:.1f} s)"}
@@ -175,18 +176,19 @@ def run_reference(args):
     spec, model, S, warm, P, T = build_inputs(args.workload, pkg, synth)
     N = oracle_null_space(S)
     threads = os.cpu_count() or 1
+    prob = oracle.Problem(model, warm, N)
     # each step: a bounded chain sample of the workload sized to ~8 s
     t0 = time.perf_counter()
-    oracle.sample(model, warm, N, args.seed, threads, 20, chain_offset=10**9, threads=threads)
-    per_round = (time.perf_counter() - t0) / 20
+    prob.sample(args.seed, threads, 50, chain_offset=10**9, threads=threads)
+    per_round = (time.perf_counter() - t0) / 50
     rounds = max(1, int(8.0 / max(per_round * T, 1e-9)))
     Pstep = threads * rounds
     for w in range(args.warmup):
-        oracle.sample(model, warm, N, args.seed + w, threads, min(T, 50), threads=threads)
+        prob.sample(args.seed + w, threads, min(T, 50), threads=threads)
     times, acc = [], 0
     for k in range(args.steps):
         t0 = time.perf_counter()
-        _, st = oracle.sample(model, warm, N, args.seed + 100 + k, Pstep, T, chain_offset=k * Pstep, threads=threads)
+        _, st = prob.sample(args.seed + 100 + k, Pstep, T, chain_offset=k * Pstep, threads=threads)
         times.append(time.perf_counter() - t0)
         acc += st["accepted"]
     total = sum(times)

@@ -110,17 +110,21 @@ def step_uniform(seed, chain, step):
 
 def csr(n_mets, row, col, val):
     """CSR of S from COO (duplicates summed, zeros dropped), rows then columns ascending."""
-    S = {}
-    for r, c, v in zip(np.asarray(row).tolist(), np.asarray(col).tolist(), np.asarray(val).tolist()):
-        S[(r, c)] = S.get((r, c), 0.0) + v
-    keys = sorted(k for k, v in S.items() if v != 0.0)
+    row = np.asarray(row, dtype=np.int64)
+    col = np.asarray(col, dtype=np.int64)
+    val = np.asarray(val, dtype=np.float64)
+    n_cols = int(col.max()) + 1 if col.size else 1
+    key = row * n_cols + col
+    uk, inv = np.unique(key, return_inverse=True)
+    sums = np.zeros(uk.size)
+    np.add.at(sums, inv, val)
+    keep = sums != 0.0
+    uk, sums = uk[keep], sums[keep]
+    r = (uk // n_cols).astype(np.int64)
     row_ptr = np.zeros(n_mets + 1, dtype=np.int32)
-    for r, _ in keys:
-        row_ptr[r + 1] += 1
+    np.add.at(row_ptr, r + 1, 1)
     row_ptr = np.cumsum(row_ptr).astype(np.int32)
-    col_idx = np.array([c for _, c in keys], dtype=np.int32)
-    vals = np.array([S[k] for k in keys], dtype=np.float64)
-    return row_ptr, col_idx, vals
+    return row_ptr, (uk % n_cols).astype(np.int32), sums
 
 
 def centre(warmup):
@@ -131,26 +135,42 @@ def centre(warmup):
     return out
 
 
+class Problem:
+    """A model, its warmup points and a null-space basis prepared once for the C oracle."""
+
+    def __init__(self, model, warmup, N, centre_point=None):
+        n = model.n_rxns
+        self.n = n
+        self.w = np.asfortranarray(np.asarray(warmup, dtype=np.float64))
+        self.N = np.asfortranarray(np.asarray(N, dtype=np.float64).reshape(n, -1))
+        self.rp, self.ci, self.vv = csr(model.n_mets, model.row, model.col, model.val)
+        self.lb = np.ascontiguousarray(model.lb, dtype=np.float64)
+        self.ub = np.ascontiguousarray(model.ub, dtype=np.float64)
+        self.c0 = centre(self.w) if centre_point is None else np.ascontiguousarray(centre_point, dtype=np.float64)
+        dp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))  # noqa: E731
+        ip = lambda a: a.ctypes.data_as(C.POINTER(C.c_int32))  # noqa: E731
+        self.pb = _Problem(n, model.n_mets, self.w.shape[1], dp(self.w), dp(self.lb), dp(self.ub), ip(self.rp),
+                           ip(self.ci), dp(self.vv), self.N.shape[1], dp(self.N), dp(self.c0))
+
+    def sample(self, seed, n_points, n_steps, chain_offset=0, check_period=10, max_attempts=100000, centre_offset=0,
+               threads=0, residual_tol=1e-9, max_min_tol=1e-9, u_tol=1e-9, d_tol=1e-14):
+        """Returns ((n, P) points, stats dict)."""
+        op = _Options(check_period, max_attempts, centre_offset, threads, residual_tol, max_min_tol, u_tol, d_tol)
+        out = np.zeros((self.n, n_points))
+        st = _Stats()
+        rc = lib().oracle_sample(C.byref(self.pb), C.byref(op), seed, chain_offset, n_points, n_steps,
+                                 out.ctypes.data_as(C.POINTER(C.c_double)), C.byref(st))
+        if rc != 0:
+            raise RuntimeError(f"oracle_sample failed ({rc})")
+        return out, {k: getattr(st, k) for k, _ in st._fields_}
+
+
 def sample(model, warmup, N, seed, n_points, n_steps, chain_offset=0, check_period=10, max_attempts=100000,
            centre_offset=0, threads=0, residual_tol=1e-9, max_min_tol=1e-9, u_tol=1e-9, d_tol=1e-14,
            centre_point=None):
     """Run the C oracle.  model: object with n_rxns, n_mets, row, col, val, lb, ub.
     warmup: (n, W); N: (n, d).  Returns ((n, P) points, stats dict)."""
-    n = model.n_rxns
-    w = np.asfortranarray(np.asarray(warmup, dtype=np.float64))
-    Nf = np.asfortranarray(np.asarray(N, dtype=np.float64).reshape(n, -1))
-    rp, ci, vv = csr(model.n_mets, model.row, model.col, model.val)
-    lb = np.ascontiguousarray(model.lb, dtype=np.float64)
-    ub = np.ascontiguousarray(model.ub, dtype=np.float64)
-    c0 = centre(w) if centre_point is None else np.ascontiguousarray(centre_point, dtype=np.float64)
-    dp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))  # noqa: E731
-    ip = lambda a: a.ctypes.data_as(C.POINTER(C.c_int32))  # noqa: E731
-    pb = _Problem(n, model.n_mets, w.shape[1], dp(w), dp(lb), dp(ub), ip(rp), ip(ci), dp(vv), Nf.shape[1], dp(Nf),
-                  dp(c0))
-    op = _Options(check_period, max_attempts, centre_offset, threads, residual_tol, max_min_tol, u_tol, d_tol)
-    out = np.zeros((n, n_points))
-    st = _Stats()
-    rc = lib().oracle_sample(C.byref(pb), C.byref(op), seed, chain_offset, n_points, n_steps, dp(out), C.byref(st))
-    if rc != 0:
-        raise RuntimeError(f"oracle_sample failed ({rc})")
-    return out, {k: getattr(st, k) for k, _ in st._fields_}
+    return Problem(model, warmup, N, centre_point).sample(
+        seed, n_points, n_steps, chain_offset=chain_offset, check_period=check_period, max_attempts=max_attempts,
+        centre_offset=centre_offset, threads=threads, residual_tol=residual_tol, max_min_tol=max_min_tol,
+        u_tol=u_tol, d_tol=d_tol)
