@@ -278,6 +278,46 @@ achr_status upload_null_space(achr_ctx *ctx, const double *N, int d) {
     return ACHR_OK;
 }
 
+// FEASIBLE mode: project the warmup points onto the span of N in FP64,
+// W <- N (N^T W) (cuBLAS), then recompute the centre.  %f-rounded warmup CSVs
+// carry |S w| ~ 1e-6; after this the sampling loop starts on null(S).
+achr_status prepare_warmup_and_centre(achr_ctx *ctx) {
+    const int n = ctx->n, W = ctx->W, d = ctx->d;
+    if (ctx->opt.mode == ACHR_MODE_FEASIBLE && d > 0) {
+        cublasHandle_t cb = nullptr;
+        if (cublasCreate(&cb) != CUBLAS_STATUS_SUCCESS) return fail(ACHR_ERR_CUDA, "cublasCreate failed");
+        const double one = 1.0, zero = 0.0;
+        const int chunk = 4096;  // warmup columns per GEMM pair (bounds the d x chunk temporary)
+        DevBuf<double> Y;
+        cudaError_t e = Y.alloc((size_t)d * (size_t)std::min(chunk, W));
+        if (e != cudaSuccess) {
+            cublasDestroy(cb);
+            return cuda_fail(e, "cudaMalloc(projection temporary)");
+        }
+        for (int j0 = 0; j0 < W; j0 += chunk) {
+            const int nc = std::min(chunk, W - j0);
+            double *Wj = ctx->warmup.p + (size_t)j0 * ctx->ldw;
+            cublasStatus_t bs = cublasDgemm(cb, CUBLAS_OP_T, CUBLAS_OP_N, d, nc, n, &one, ctx->N.p, n, Wj, ctx->ldw,
+                                            &zero, Y.p, d);
+            if (bs == CUBLAS_STATUS_SUCCESS)
+                bs = cublasDgemm(cb, CUBLAS_OP_N, CUBLAS_OP_N, n, nc, d, &one, ctx->N.p, n, Y.p, d, &zero, Wj,
+                                 ctx->ldw);
+            if (bs != CUBLAS_STATUS_SUCCESS) {
+                cublasDestroy(cb);
+                return fail(ACHR_ERR_CUDA, "cublasDgemm (warmup projection) failed");
+            }
+        }
+        cublasDestroy(cb);
+    }
+    ACHR_CUDA_TRY(cudaMemset(ctx->c0.p, 0, sizeof(double) * ctx->np));
+    ACHR_CUDA_TRY(cudaMemset(ctx->A0.p, 0, sizeof(double) * ctx->np));
+    centre_kernel<<<(n + 127) / 128, 128>>>(n, W, ctx->ldw, ctx->warmup.p, ctx->opt.centre_offset, ctx->c0.p,
+                                            ctx->A0.p);
+    ACHR_CUDA_TRY(cudaGetLastError());
+    ACHR_CUDA_TRY(cudaDeviceSynchronize());
+    return ACHR_OK;
+}
+
 achr_status read_counters(achr_ctx *ctx, achr_stats *stats, float ms) {
     unsigned long long c[achr::CNT_SLOTS];
     ACHR_CUDA_TRY(cudaMemcpy(c, ctx->counters.p, sizeof(c), cudaMemcpyDeviceToHost));
@@ -445,15 +485,12 @@ achr_status achr_create(const achr_model *model, const double *warmup, int32_t n
     st = upload_null_space(ctx, Nh.data(), d);
     if (st != ACHR_OK) return st;
 
-    // Centre of the warmup points and the centre accumulator.
+    // Centre of the warmup points and the centre accumulator (after the
+    // FEASIBLE-mode projection of the warmup points).
     ACHR_CUDA_TRY(ctx->c0.alloc(np));
     ACHR_CUDA_TRY(ctx->A0.alloc(np));
-    ACHR_CUDA_TRY(cudaMemset(ctx->c0.p, 0, sizeof(double) * np));
-    ACHR_CUDA_TRY(cudaMemset(ctx->A0.p, 0, sizeof(double) * np));
-    centre_kernel<<<(n + 127) / 128, 128>>>(n, n_warmup, ctx->ldw, ctx->warmup.p, opt.centre_offset, ctx->c0.p,
-                                            ctx->A0.p);
-    ACHR_CUDA_TRY(cudaGetLastError());
-    ACHR_CUDA_TRY(cudaDeviceSynchronize());
+    st = prepare_warmup_and_centre(ctx);
+    if (st != ACHR_OK) return st;
 
     owned = nullptr;  // release from the guard
     *out = ctx;
@@ -463,7 +500,9 @@ achr_status achr_create(const achr_model *model, const double *warmup, int32_t n
 
 achr_status achr_set_null_space(achr_ctx *ctx, const double *N, int32_t d) {
     if (!ctx || (!N && d > 0) || d < 0 || d > ctx->n) return fail(ACHR_ERR_INVALID, "bad null-space arguments");
-    return upload_null_space(ctx, N, d);
+    achr_status st = upload_null_space(ctx, N, d);
+    if (st != ACHR_OK || ctx->opt.mode != ACHR_MODE_FEASIBLE) return st;
+    return prepare_warmup_and_centre(ctx);  // re-project the warmup points onto the new basis
 }
 
 achr_status achr_get_null_space_dim(const achr_ctx *ctx, int32_t *d) {

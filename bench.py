@@ -52,6 +52,8 @@ def parse_args():
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target length of the CPU baseline sample")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-case", type=int, nargs=2, metavar=("CHAINS", "STEPS"),
+                    help="run two launches of CHAINS x STEPS of the workload and print their times (ncu captures)")
     return ap.parse_args()
 
 
@@ -327,8 +329,33 @@ def run_gpu(args):
     return 0
 
 
+def run_profile_case(args):
+    """Two launches of a small chain sample of the workload (the second is the one to capture)."""
+    import torch
+
+    import __graft_entry__ as ge
+
+    pkg = ge.load_package()
+    pkg.lib()
+    import importlib
+    synth = importlib.import_module("achr_gb300.synthetic")
+    spec, model, S, warm, _, _ = build_inputs(args.workload, pkg, synth)
+    P, T = args.profile_case
+    smp = pkg.Sampler(model, warm)
+    out = torch.empty((spec.n_rxns, P), dtype=torch.float64, device="cuda")
+    stream = torch.cuda.current_stream().cuda_stream
+    for k in range(2):
+        st = smp.sample_device(P, T, out.data_ptr(), P, stream, seed=args.seed + k, with_stats=True)
+        print(f"launch {k}: {st['kernel_ms']:.3f} ms, {P * T / (st['kernel_ms'] * 1e-3):.4e} chain-steps/s, "
+              f"{st['exact_evals'] / max(1, P * T):.3f} FP64 ratio evaluations per step", flush=True)
+    smp.close()
+    return 0
+
+
 def main():
     args = parse_args()
+    if args.profile_case:
+        return run_profile_case(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_gpu(args)

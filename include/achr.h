@@ -107,7 +107,9 @@ achr_status achr_create(const achr_model *model, const double *warmup, int32_t n
 
 /* Replace the context's null-space basis with a caller-supplied one (n x d,
  * column-major, host memory).  The reference computes it internally
- * (ACHRCuda.cu:698-704); this lets a caller pin N across implementations. */
+ * (ACHRCuda.cu:698-704); this lets a caller pin N across implementations.
+ * In ACHR_MODE_FEASIBLE the warmup points are projected onto the new basis
+ * and the centre is recomputed. */
 achr_status achr_set_null_space(achr_ctx *ctx, const double *N, int32_t d);
 
 /* Null-space dimension d and the basis itself (n x d column-major, host). */

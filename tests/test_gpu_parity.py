@@ -114,6 +114,9 @@ def test_feasible_mode_emits_feasible_points(pkg, small_model, golden):
     lb, ub = golden["lb"][:, None], golden["ub"][:, None]
     assert (pts >= lb - 1e-9).all() and (pts <= ub + 1e-9).all()
     assert st["max_residual"] <= 1e-8
+    # the %f-rounded warmups were projected onto null(S) at set-up, so the
+    # in-loop residual checks no longer find anything to reproject
+    assert st["checks"] > 0 and st["reprojections"] == 0
 
 
 def test_stuck_chain_reported(pkg):
