@@ -79,6 +79,18 @@ class Stats(C.Structure):
         return {name: getattr(self, name) for name, _ in self._fields_}
 
 
+class DeviceModel(C.Structure):
+    """achr_device_model: a model already in device memory (pointers are device addresses)."""
+    _fields_ = [
+        ("n_rxns", C.c_int32), ("n_mets", C.c_int32), ("n_warmup", C.c_int32), ("null_dim", C.c_int32),
+        ("ld_warmup", C.c_int64), ("warmup", C.c_void_p), ("lb", C.c_void_p), ("ub", C.c_void_p),
+        ("row_ptr", C.c_void_p), ("col_idx", C.c_void_p), ("val", C.c_void_p), ("N", C.c_void_p),
+    ]
+
+
+NOALLOC_MAX_RXNS = 8192
+
+
 # Every symbol include/achr.h declares, with its ctypes signature.
 _SIGNATURES = {
     "achr_default_options": (None, [C.POINTER(Options)]),
@@ -93,6 +105,8 @@ _SIGNATURES = {
     "achr_sample_device": (C.c_int, [C.c_void_p, C.c_uint64, C.c_uint64, C.c_int32, C.c_int32, C.c_void_p,
                                      C.c_int64, C.c_void_p, C.POINTER(Stats)]),
     "achr_destroy": (None, [C.c_void_p]),
+    "achr_sample_noalloc": (C.c_int, [C.POINTER(DeviceModel), C.POINTER(Options), C.c_uint64, C.c_uint64, C.c_int32,
+                                      C.c_int32, C.c_void_p, C.c_int64, C.c_void_p, C.POINTER(Stats)]),
     "achr_read_mps": (C.c_int, [C.c_char_p, C.POINTER(ModelBuf)]),
     "achr_free_model": (None, [C.POINTER(ModelBuf)]),
     "achr_read_warmup_csv": (C.c_int, [C.c_char_p, C.c_int32, C.POINTER(C.POINTER(C.c_double)),
@@ -306,6 +320,16 @@ class Sampler:
         _check(lib().achr_sample_device(self._ctx, seed, chain_offset, n_points, n_steps, C.c_void_p(d_out), ld_out,
                                         C.c_void_p(stream), C.byref(st) if st is not None else None))
         return st.as_dict() if st is not None else None
+
+
+def sample_noalloc(model: DeviceModel, n_points: int, n_steps: int, d_out: int, ld_out: int, stream: int = 0,
+                   seed: int = 0, chain_offset: int = 0, options: Optional[Options] = None) -> dict:
+    """Sample through achr_sample_noalloc (no allocation by the library); returns the stats."""
+    st = Stats()
+    opt = options if options is not None else default_options()
+    _check(lib().achr_sample_noalloc(C.byref(model), C.byref(opt), seed, chain_offset, n_points, n_steps,
+                                     C.c_void_p(d_out), ld_out, C.c_void_p(stream), C.byref(st)))
+    return st.as_dict()
 
 
 def exported_symbols() -> list[str]:

@@ -140,6 +140,45 @@ achr_status achr_sample_device(achr_ctx *ctx, uint64_t seed, uint64_t chain_offs
 /* Release every device and host resource of the context. */
 void achr_destroy(achr_ctx *ctx);
 
+/* ---- Sampling without any allocation ---- */
+
+/* Largest model (reactions) achr_sample_noalloc accepts: its working data sits
+ * in a fixed array of about 40 bytes per reaction (321 KB) that every GPU
+ * loading the library keeps until the process exits. */
+#define ACHR_NOALLOC_MAX_RXNS 8192
+
+/* A model already resident in device memory (all pointers are device pointers). */
+typedef struct {
+    int32_t n_rxns;           /* n, at most ACHR_NOALLOC_MAX_RXNS */
+    int32_t n_mets;           /* m */
+    int32_t n_warmup;         /* W */
+    int32_t null_dim;         /* d, columns of N */
+    int64_t ld_warmup;        /* leading dimension of warmup in doubles: even and >= n_rxns */
+    const double *warmup;     /* ld_warmup x W, column j = warmup point j; 16-byte aligned */
+    const double *lb, *ub;    /* n bounds */
+    const int32_t *row_ptr;   /* CSR of S: m + 1 offsets */
+    const int32_t *col_idx;   /* nnz column indices in [0, n) */
+    const double *val;        /* nnz coefficients */
+    const double *N;          /* n x d column-major null-space basis */
+} achr_device_model;
+
+/* No counterpart in the reference (which allocates all its buffers itself).
+ * Same sampling as achr_sample_device, for callers that may not allocate GPU
+ * memory (code inside another framework's memory pool or a pre-sized arena,
+ * or a repeated path that must not add allocations): inputs and the n x P
+ * output (leading dimension ld_out) are the caller's device buffers, and the
+ * library calls no cudaMalloc, cudaFree or allocating library routine.  Its
+ * working data lives in one fixed device array shared by all calls; the first
+ * call on each device looks up that array's address (make it before any
+ * stream capture); calls whose GPU work overlaps race on it and must be
+ * serialised.  Models above ACHR_NOALLOC_MAX_RXNS reactions are rejected with
+ * ACHR_ERR_UNSUPPORTED.  The null space is the caller's (as with
+ * achr_set_null_space); in ACHR_MODE_FEASIBLE only the final projection of
+ * emitted points is applied.  Synchronises the stream; stats->kernel_ms is 0. */
+achr_status achr_sample_noalloc(const achr_device_model *model, const achr_options *opt, uint64_t seed,
+                                uint64_t chain_offset, int32_t n_points, int32_t n_steps, double *d_points_out,
+                                int64_t ld_out, void *stream, achr_stats *stats);
+
 /* ---- Host input/output used by the ACHRCuda CLI (ACHRCuda.cu:558-689, 744-756) ---- */
 
 /* Parsed model owned by the library (free with achr_free_model). */
