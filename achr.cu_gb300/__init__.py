@@ -91,6 +91,17 @@ class DeviceModel(C.Structure):
 NOALLOC_MAX_RXNS = 8192
 
 
+class BatchStats(C.Structure):
+    _fields_ = [
+        ("graph_ms", C.c_double), ("load_imbalance", C.c_double), ("accepted", C.c_int64), ("rejected", C.c_int64),
+        ("reprojections", C.c_int64), ("stuck_chains", C.c_int64), ("max_residual", C.c_double),
+        ("max_bound_violation", C.c_double),
+    ]
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
 # Every symbol include/achr.h declares, with its ctypes signature.
 _SIGNATURES = {
     "achr_default_options": (None, [C.POINTER(Options)]),
@@ -105,6 +116,10 @@ _SIGNATURES = {
     "achr_sample_device": (C.c_int, [C.c_void_p, C.c_uint64, C.c_uint64, C.c_int32, C.c_int32, C.c_void_p,
                                      C.c_int64, C.c_void_p, C.POINTER(Stats)]),
     "achr_destroy": (None, [C.c_void_p]),
+    "achr_autotune": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
+    "achr_sample_batch": (C.c_int, [C.POINTER(C.c_void_p), C.c_int32, C.POINTER(C.c_int32), C.c_int32, C.c_uint64,
+                                    C.POINTER(C.c_void_p), C.POINTER(C.c_int64), C.c_void_p, C.POINTER(BatchStats),
+                                    C.POINTER(C.c_double)]),
     "achr_sample_noalloc": (C.c_int, [C.POINTER(DeviceModel), C.POINTER(Options), C.c_uint64, C.c_uint64, C.c_int32,
                                       C.c_int32, C.c_void_p, C.c_int64, C.c_void_p, C.POINTER(Stats)]),
     "achr_read_mps": (C.c_int, [C.c_char_p, C.POINTER(ModelBuf)]),
@@ -313,6 +328,13 @@ class Sampler:
         _check(lib().achr_sample(self._ctx, seed, chain_offset, n_points, n_steps, _dptr(out), C.byref(st)))
         return out, st.as_dict()
 
+    def autotune(self) -> int:
+        """Pick the fastest chain-kernel configuration for this model; returns threads per chain."""
+        t = C.c_int32()
+        _check(lib().achr_autotune(self._ctx, C.byref(t)))
+        self.options.threads_per_chain = t.value
+        return t.value
+
     def sample_device(self, n_points: int, n_steps: int, d_out: int, ld_out: int, stream: int = 0, seed: int = 0,
                       chain_offset: int = 0, with_stats: bool = False) -> Optional[dict]:
         """Queue sampling into device memory d_out (n x ld_out row-major) on a CUDA stream."""
@@ -330,6 +352,20 @@ def sample_noalloc(model: DeviceModel, n_points: int, n_steps: int, d_out: int, 
     _check(lib().achr_sample_noalloc(C.byref(model), C.byref(opt), seed, chain_offset, n_points, n_steps,
                                      C.c_void_p(d_out), ld_out, C.c_void_p(stream), C.byref(st)))
     return st.as_dict()
+
+
+def sample_batch(samplers, n_points, n_steps: int, d_outs, ld_outs, stream: int = 0, seed: int = 0):
+    """Sample several models in one CUDA-graph launch (achr_sample_batch).
+    Returns (batch stats dict, per-model finish times in ms)."""
+    k = len(samplers)
+    ctxs = (C.c_void_p * k)(*[s._ctx for s in samplers])
+    pts = (C.c_int32 * k)(*n_points)
+    outs = (C.c_void_p * k)(*d_outs)
+    lds = (C.c_int64 * k)(*ld_outs)
+    ms = (C.c_double * k)()
+    st = BatchStats()
+    _check(lib().achr_sample_batch(ctxs, k, pts, n_steps, seed, outs, lds, C.c_void_p(stream), C.byref(st), ms))
+    return st.as_dict(), list(ms)
 
 
 def exported_symbols() -> list[str]:

@@ -24,7 +24,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-Wall", "-Wno-unused-function"]
 
-CU_SOURCES = ["achr_chain_kernel.cu", "achr_capi.cu", "achr_noalloc.cu"]
+CU_SOURCES = ["achr_chain_cfg_small.cu", "achr_chain_cfg_large.cu", "achr_chain_launch.cu", "achr_capi.cu",
+              "achr_noalloc.cu"]
 CXX_SOURCES = ["achr_io.cpp"]
 
 

@@ -7,6 +7,8 @@
 
 #include <algorithm>
 #include <cmath>
+#include <map>
+#include <mutex>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -92,6 +94,14 @@ float f32_down(double v) {
     float f = (float)v;
     if ((double)f > v) f = std::nextafter(f, -INFINITY);
     return f;
+}
+
+// Writes the global nanosecond timer (used to time each model's branch of a
+// batched graph).
+__global__ void stamp_kernel(unsigned long long *slot) {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    *slot = t;
 }
 
 __global__ void centre_kernel(int n, int W, int ldw, const double *__restrict__ warmup, int centre_offset,
@@ -318,6 +328,9 @@ achr_status prepare_warmup_and_centre(achr_ctx *ctx) {
     return ACHR_OK;
 }
 
+ChainArgs chain_args(const achr_ctx *ctx, uint64_t seed, uint64_t chain_offset, int32_t n_points, int32_t n_steps,
+                     double *d_points_out, int64_t ld_out);
+
 achr_status read_counters(achr_ctx *ctx, achr_stats *stats, float ms) {
     unsigned long long c[achr::CNT_SLOTS];
     ACHR_CUDA_TRY(cudaMemcpy(c, ctx->counters.p, sizeof(c), cudaMemcpyDeviceToHost));
@@ -407,8 +420,9 @@ achr_status achr_create(const achr_model *model, const double *warmup, int32_t n
 
     // Per-reaction arrays are padded to the kernel's block size x elements per
     // thread; padding entries are fixed at 0 (lb = ub = 0) and never move.
-    const int np = achr::chain_padded_length(n, opt.threads_per_chain);
-    if (np == 0) return fail(ACHR_ERR_UNSUPPORTED, "no chain-kernel configuration for n_rxns with this threads_per_chain");
+    const int np_cfg = achr::chain_padded_length(n, opt.threads_per_chain);
+    if (np_cfg == 0) return fail(ACHR_ERR_UNSUPPORTED, "no chain-kernel configuration for n_rxns with this threads_per_chain");
+    const int np = std::max(np_cfg, achr::chain_alloc_length(n));  // room for every autotuning candidate
     ctx->np = np;
     // Padding reactions have lb = ub = 0 in FP64 and the FP32 box (-1, 1), so
     // their (zero) coordinate is never a candidate and never needs a clip.
@@ -531,6 +545,36 @@ achr_status achr_sample_device(achr_ctx *ctx, uint64_t seed, uint64_t chain_offs
     if (n_points > 0 && (!d_points_out || ld_out < n_points)) return fail(ACHR_ERR_INVALID, "bad output buffer");
     if (chain_offset + (uint64_t)n_points < chain_offset) return fail(ACHR_ERR_INVALID, "chain ids overflow");
     cudaStream_t s = (cudaStream_t)stream;
+    const ChainArgs a = chain_args(ctx, seed, chain_offset, n_points, n_steps, d_points_out, ld_out);
+    ACHR_CUDA_TRY(cudaMemsetAsync(ctx->counters.p, 0, sizeof(unsigned long long) * achr::CNT_SLOTS, s));
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (stats) {
+        ACHR_CUDA_TRY(cudaEventCreate(&e0));
+        ACHR_CUDA_TRY(cudaEventCreate(&e1));
+        ACHR_CUDA_TRY(cudaEventRecord(e0, s));
+    }
+    cudaError_t e = achr::launch_chains(a, ctx->opt.threads_per_chain, s);
+    if (e != cudaSuccess) {
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+        return cuda_fail(e, "chain kernel launch");
+    }
+    if (!stats) return ACHR_OK;
+    ACHR_CUDA_TRY(cudaEventRecord(e1, s));
+    ACHR_CUDA_TRY(cudaEventSynchronize(e1));
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return read_counters(ctx, stats, ms);
+}
+
+}  // extern "C"
+
+namespace {
+
+ChainArgs chain_args(const achr_ctx *ctx, uint64_t seed, uint64_t chain_offset, int32_t n_points, int32_t n_steps,
+                     double *d_points_out, int64_t ld_out) {
     ChainArgs a{};
     a.n = ctx->n;
     a.m = ctx->m;
@@ -569,28 +613,12 @@ achr_status achr_sample_device(achr_ctx *ctx, uint64_t seed, uint64_t chain_offs
     a.d_tol = ctx->opt.d_tol;
     a.feasibility_tol = ctx->opt.feasibility_tol;
     a.counters = ctx->counters.p;
-    ACHR_CUDA_TRY(cudaMemsetAsync(ctx->counters.p, 0, sizeof(unsigned long long) * achr::CNT_SLOTS, s));
-    cudaEvent_t e0 = nullptr, e1 = nullptr;
-    if (stats) {
-        ACHR_CUDA_TRY(cudaEventCreate(&e0));
-        ACHR_CUDA_TRY(cudaEventCreate(&e1));
-        ACHR_CUDA_TRY(cudaEventRecord(e0, s));
-    }
-    cudaError_t e = achr::launch_chains(a, ctx->opt.threads_per_chain, s);
-    if (e != cudaSuccess) {
-        if (e0) cudaEventDestroy(e0);
-        if (e1) cudaEventDestroy(e1);
-        return cuda_fail(e, "chain kernel launch");
-    }
-    if (!stats) return ACHR_OK;
-    ACHR_CUDA_TRY(cudaEventRecord(e1, s));
-    ACHR_CUDA_TRY(cudaEventSynchronize(e1));
-    float ms = 0.0f;
-    cudaEventElapsedTime(&ms, e0, e1);
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
-    return read_counters(ctx, stats, ms);
+    return a;
 }
+
+}  // namespace
+
+extern "C" {
 
 achr_status achr_sample(achr_ctx *ctx, uint64_t seed, uint64_t chain_offset, int32_t n_points, int32_t n_steps,
                         double *points_out, achr_stats *stats) {
@@ -608,5 +636,187 @@ achr_status achr_sample(achr_ctx *ctx, uint64_t seed, uint64_t chain_offset, int
 }
 
 void achr_destroy(achr_ctx *ctx) { delete ctx; }
+
+}  // extern "C"
+
+namespace {
+
+// Autotuning results per (default padded length, device): threads per chain.
+std::mutex g_tune_mutex;
+std::map<std::pair<int, int>, int> g_tune_cache;
+
+struct StreamSet {
+    std::vector<cudaStream_t> streams;
+    std::vector<cudaEvent_t> events;
+    ~StreamSet() {
+        for (cudaStream_t s : streams) cudaStreamDestroy(s);
+        for (cudaEvent_t e : events) cudaEventDestroy(e);
+    }
+};
+
+}  // namespace
+
+extern "C" {
+
+achr_status achr_autotune(achr_ctx *ctx, int32_t *threads_per_chain_out) {
+    if (!ctx) return fail(ACHR_ERR_INVALID, "ctx is NULL");
+    int dev = 0;
+    ACHR_CUDA_TRY(cudaGetDevice(&dev));
+    const std::pair<int, int> key(achr::chain_padded_length(ctx->n, 0), dev);
+    {
+        std::lock_guard<std::mutex> lock(g_tune_mutex);
+        auto it = g_tune_cache.find(key);
+        if (it != g_tune_cache.end()) {
+            ctx->opt.threads_per_chain = it->second;
+            if (threads_per_chain_out) *threads_per_chain_out = it->second;
+            return ACHR_OK;
+        }
+    }
+    int cand[8];
+    const int nc = achr::chain_candidates(ctx->n, ctx->np, cand, 8);
+    if (nc == 0) return fail(ACHR_ERR_UNSUPPORTED, "no chain-kernel configuration to tune");
+    int sms = 0;
+    ACHR_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    // A short run that fills the GPU a few times over: 4 chains per SM, 32 steps.
+    const int P = 4 * sms, T = 32;
+    const size_t need = (size_t)ctx->n * (size_t)P;
+    if (ctx->points.count < need) ACHR_CUDA_TRY(ctx->points.alloc(need));
+    const int saved = ctx->opt.threads_per_chain;
+    int best = cand[0];
+    double best_ms = 1e300;
+    for (int c = 0; c < nc; ++c) {
+        ctx->opt.threads_per_chain = cand[c];
+        achr_stats st;
+        achr_status r = achr_sample_device(ctx, 0x5eedull, 0, P, 4, ctx->points.p, P, nullptr, &st);  // warm-up
+        if (r == ACHR_OK) r = achr_sample_device(ctx, 0x5eedull, 0, P, T, ctx->points.p, P, nullptr, &st);
+        if (r != ACHR_OK) {
+            ctx->opt.threads_per_chain = saved;
+            return r;
+        }
+        if (st.kernel_ms < best_ms) {
+            best_ms = st.kernel_ms;
+            best = cand[c];
+        }
+    }
+    ctx->opt.threads_per_chain = best;
+    {
+        std::lock_guard<std::mutex> lock(g_tune_mutex);
+        g_tune_cache[key] = best;
+    }
+    if (threads_per_chain_out) *threads_per_chain_out = best;
+    return ACHR_OK;
+}
+
+achr_status achr_sample_batch(achr_ctx *const *ctxs, int32_t n_models, const int32_t *n_points, int32_t n_steps,
+                              uint64_t seed, double *const *d_points_out, const int64_t *ld_out, void *stream,
+                              achr_batch_stats *stats, double *model_ms_out) {
+    if (!ctxs || !n_points || !d_points_out || !ld_out || n_models <= 0 || n_steps < 0)
+        return fail(ACHR_ERR_INVALID, "bad batch arguments");
+    int dev = 0, sms = 0;
+    ACHR_CUDA_TRY(cudaGetDevice(&dev));
+    ACHR_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    // Work of each model (padded elements x chain-steps) sets its share of the SMs.
+    std::vector<double> work((size_t)n_models);
+    std::vector<int> per_sm((size_t)n_models);
+    std::vector<uint64_t> offset((size_t)n_models);
+    double total = 0.0;
+    uint64_t off = 0;
+    for (int k = 0; k < n_models; ++k) {
+        achr_ctx *c = ctxs[k];
+        if (!c || n_points[k] < 0 || (n_points[k] > 0 && (!d_points_out[k] || ld_out[k] < n_points[k])))
+            return fail(ACHR_ERR_INVALID, "bad batch entry " + std::to_string(k));
+        const ChainArgs a0 = chain_args(c, seed, 0, 0, n_steps, d_points_out[k], ld_out[k]);
+        cudaError_t e = achr::launch_chains(a0, c->opt.threads_per_chain, nullptr, 0, &per_sm[(size_t)k]);
+        if (e != cudaSuccess) return cuda_fail(e, "chain kernel configuration");
+        work[(size_t)k] = (double)n_points[k] * (double)n_steps *
+                          (double)achr::chain_padded_length(c->n, c->opt.threads_per_chain);
+        total += work[(size_t)k];
+        offset[(size_t)k] = off;  // disjoint chain ids: model k uses ids off .. off + P_k - 1
+        off += (uint64_t)n_points[k];
+    }
+    cudaStream_t main = (cudaStream_t)stream;
+    StreamSet ss;
+    if (main == nullptr) {  // the legacy default stream cannot be captured: use a private stream
+        cudaStream_t own = nullptr;
+        ACHR_CUDA_TRY(cudaStreamCreateWithFlags(&own, cudaStreamNonBlocking));
+        ss.streams.push_back(own);
+        main = own;
+    }
+    const size_t first = ss.streams.size();
+    ss.streams.resize(first + (size_t)n_models, nullptr);
+    ss.events.resize((size_t)n_models + 3, nullptr);
+    for (size_t q = first; q < ss.streams.size(); ++q)
+        ACHR_CUDA_TRY(cudaStreamCreateWithFlags(&ss.streams[q], cudaStreamNonBlocking));
+    for (auto &ev : ss.events) ACHR_CUDA_TRY(cudaEventCreate(&ev));
+    cudaEvent_t fork = ss.events[(size_t)n_models], t0 = ss.events[(size_t)n_models + 1],
+                t1 = ss.events[(size_t)n_models + 2];
+    DevBuf<unsigned long long> stamps;  // [0, n_models): each model's finish, [n_models]: graph start
+    ACHR_CUDA_TRY(stamps.alloc((size_t)n_models + 1));
+    // One graph: fork, one persistent chain kernel per model on its own stream
+    // (grid = its share of the SMs x resident CTAs), join.
+    cudaGraph_t graph = nullptr;
+    ACHR_CUDA_TRY(cudaStreamBeginCapture(main, cudaStreamCaptureModeThreadLocal));
+    stamp_kernel<<<1, 1, 0, main>>>(stamps.p + n_models);
+    cudaError_t ce = cudaGetLastError();
+    if (ce == cudaSuccess) ce = cudaEventRecord(fork, main);
+    for (int k = 0; k < n_models && ce == cudaSuccess; ++k) {
+        cudaStream_t sk = ss.streams[first + (size_t)k];
+        achr_ctx *c = ctxs[k];
+        ce = cudaStreamWaitEvent(sk, fork, 0);
+        if (ce == cudaSuccess)
+            ce = cudaMemsetAsync(c->counters.p, 0, sizeof(unsigned long long) * achr::CNT_SLOTS, sk);
+        const double share = total > 0 ? work[(size_t)k] / total : 1.0 / n_models;
+        const int sm_share = std::max(1, (int)std::lround(share * sms));
+        const ChainArgs a = chain_args(c, seed, offset[(size_t)k], n_points[k], n_steps, d_points_out[k], ld_out[k]);
+        if (ce == cudaSuccess) ce = achr::launch_chains(a, c->opt.threads_per_chain, sk, sm_share * per_sm[(size_t)k]);
+        if (ce == cudaSuccess) {
+            stamp_kernel<<<1, 1, 0, sk>>>(stamps.p + k);
+            ce = cudaGetLastError();
+        }
+        if (ce == cudaSuccess) ce = cudaEventRecord(ss.events[(size_t)k], sk);
+        if (ce == cudaSuccess) ce = cudaStreamWaitEvent(main, ss.events[(size_t)k], 0);
+    }
+    cudaError_t ee = cudaStreamEndCapture(main, &graph);
+    if (ce != cudaSuccess || ee != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        return cuda_fail(ce != cudaSuccess ? ce : ee, "batched graph capture");
+    }
+    cudaGraphExec_t exec = nullptr;
+    ce = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ce != cudaSuccess) return cuda_fail(ce, "cudaGraphInstantiate");
+    ce = cudaEventRecord(t0, main);
+    if (ce == cudaSuccess) ce = cudaGraphLaunch(exec, main);
+    if (ce == cudaSuccess) ce = cudaEventRecord(t1, main);
+    if (ce == cudaSuccess) ce = cudaEventSynchronize(t1);
+    cudaGraphExecDestroy(exec);
+    if (ce != cudaSuccess) return cuda_fail(ce, "batched graph launch");
+    float total_ms = 0.0f;
+    ACHR_CUDA_TRY(cudaEventElapsedTime(&total_ms, t0, t1));
+    std::vector<unsigned long long> ts((size_t)n_models + 1);
+    ACHR_CUDA_TRY(cudaMemcpy(ts.data(), stamps.p, sizeof(unsigned long long) * ts.size(), cudaMemcpyDeviceToHost));
+    double mx = 0.0, mean = 0.0;
+    achr_batch_stats bs{};
+    for (int k = 0; k < n_models; ++k) {
+        const float mk = (float)((double)(ts[(size_t)k] - ts[(size_t)n_models]) * 1e-6);
+        if (model_ms_out) model_ms_out[k] = mk;
+        mx = std::max(mx, (double)mk);
+        mean += mk;
+        achr_stats st;
+        achr_status r = read_counters(ctxs[k], &st, mk);
+        if (r != ACHR_OK) return r;
+        bs.accepted += st.accepted;
+        bs.rejected += st.rejected;
+        bs.reprojections += st.reprojections;
+        bs.stuck_chains += st.stuck_chains;
+        bs.max_residual = std::max(bs.max_residual, st.max_residual);
+        bs.max_bound_violation = std::max(bs.max_bound_violation, st.max_bound_violation);
+    }
+    mean /= n_models;
+    bs.graph_ms = total_ms;
+    bs.load_imbalance = mx > 0 ? (mx - mean) / mx : 0.0;
+    if (stats) *stats = bs;
+    return ACHR_OK;
+}
 
 }  // extern "C"

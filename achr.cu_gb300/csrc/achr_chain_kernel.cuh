@@ -1,4 +1,7 @@
+#pragma once
 // Persistent chain kernel: the ACHR sampling hot loop on sm_103a.
+// (Template; instantiated for each block-size / elements-per-thread pair in
+// achr_chain_cfg_*.cu, dispatched by achr_chain_launch.cu.)
 //
 // Replaces the reference's chain driver and step loop (ACHRcu/ACHRCuda.cu:
 // stepPointProgress :361-385, createPoint :297-359, fillrandPoint :251-289,
@@ -256,7 +259,7 @@ constexpr int kTbl = 64;  // steps per refill of the step table
 
 // Shared memory of one CTA: xs, As, ws (NP doubles each; ws doubles as the
 // reprojection scratch), the step table and the reduction slots.
-size_t chain_smem_bytes_cfg(int np, int d, int bd) {
+inline size_t chain_smem_bytes_cfg(int np, int d, int bd) {
     (void)d;
     (void)bd;
     return sizeof(double) * 3 * (size_t)np + sizeof(StepEntry) * kTbl + 2 * sizeof(RedSlots) + 128;
@@ -784,32 +787,10 @@ __global__ void __launch_bounds__(BD, (BD <= 256 ? 2 : 1)) achr_chain_kernel(con
     }
 }
 
-// Block size / elements-per-thread ladder: the smallest padded length BD*EPT >= n.
-struct Cfg {
-    int bd, ept;
-};
-static const Cfg kLadder[] = {{32, 4}, {64, 4}, {128, 4}, {128, 8}, {256, 8}, {256, 16}, {512, 16}, {512, 32}};
-
-int chain_padded_length(int n, int threads_per_chain) {
-    for (const Cfg &c : kLadder)
-        if ((threads_per_chain == 0 || c.bd == threads_per_chain) && c.bd * c.ept >= n) return c.bd * c.ept;
-    return 0;
-}
-
-int chain_block_size(int n, int threads_per_chain) {
-    for (const Cfg &c : kLadder)
-        if ((threads_per_chain == 0 || c.bd == threads_per_chain) && c.bd * c.ept >= n) return c.bd;
-    return 0;
-}
-
-size_t chain_smem_bytes(int n, int d, int ldw, int block) {
-    (void)ldw;
-    const int np = chain_padded_length(n, block);
-    return chain_smem_bytes_cfg(np, d, block);
-}
-
+// Occupancy-sized persistent launch of one configuration.  max_ctas > 0 caps
+// the grid (batched launches share the SMs between models).
 template <int BD, int EPT>
-static cudaError_t launch_cfg(const ChainArgs &a, cudaStream_t stream) {
+cudaError_t launch_cfg(const ChainArgs &a, cudaStream_t stream, int max_ctas, int *per_sm_out) {
     const size_t smem = chain_smem_bytes_cfg(BD * EPT, a.d, BD);
     cudaError_t e = cudaFuncSetAttribute(achr_chain_kernel<BD, EPT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
@@ -818,32 +799,17 @@ static cudaError_t launch_cfg(const ChainArgs &a, cudaStream_t stream) {
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, achr_chain_kernel<BD, EPT>, BD, smem);
     if (e != cudaSuccess) return e;
     if (per_sm < 1) return cudaErrorInvalidConfiguration;
+    if (per_sm_out) *per_sm_out = per_sm;
+    if (a.P <= 0) return cudaSuccess;
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     long long grid = (long long)sms * per_sm;
+    if (max_ctas > 0 && grid > max_ctas) grid = max_ctas;
     if (grid > a.P) grid = a.P;
     if (grid < 1) return cudaSuccess;
     achr_chain_kernel<BD, EPT><<<(unsigned)grid, BD, smem, stream>>>(a);
     return cudaGetLastError();
-}
-
-cudaError_t launch_chains(const ChainArgs &a, int threads_per_chain, cudaStream_t stream) {
-    if (a.P <= 0) return cudaSuccess;
-    const int bd = chain_block_size(a.n, threads_per_chain);
-    const int np = chain_padded_length(a.n, threads_per_chain);
-    if (bd == 0 || np != a.np) return cudaErrorInvalidValue;
-    switch (np / bd * 10000 + bd) {
-        case 4 * 10000 + 32: return launch_cfg<32, 4>(a, stream);
-        case 4 * 10000 + 64: return launch_cfg<64, 4>(a, stream);
-        case 4 * 10000 + 128: return launch_cfg<128, 4>(a, stream);
-        case 8 * 10000 + 128: return launch_cfg<128, 8>(a, stream);
-        case 8 * 10000 + 256: return launch_cfg<256, 8>(a, stream);
-        case 16 * 10000 + 256: return launch_cfg<256, 16>(a, stream);
-        case 16 * 10000 + 512: return launch_cfg<512, 16>(a, stream);
-        case 32 * 10000 + 512: return launch_cfg<512, 32>(a, stream);
-        default: return cudaErrorInvalidValue;
-    }
 }
 
 }  // namespace achr

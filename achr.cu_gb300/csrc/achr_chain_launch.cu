@@ -1,0 +1,84 @@
+// Configuration ladder of the chain kernel and its dispatcher.
+//
+// A configuration is (threads per chain BD, elements per thread EPT); its
+// padded length BD * EPT must hold the model's n reactions.  For each padded
+// length there is a default configuration (used when threads_per_chain = 0)
+// and alternatives that the autotuner may pick.
+#include "achr_internal.h"
+
+namespace achr {
+
+cudaError_t launch_chain_cfg_small(int bd, int ept, const ChainArgs &a, cudaStream_t s, int max_ctas, int *per_sm);
+cudaError_t launch_chain_cfg_large(int bd, int ept, const ChainArgs &a, cudaStream_t s, int max_ctas, int *per_sm);
+
+namespace {
+
+struct Cfg {
+    int bd, ept;
+    bool dflt;
+};
+
+// Ordered by padded length; the default for each length comes first.
+const Cfg kLadder[] = {
+    {32, 4, true},   {64, 4, true},   {32, 8, false},  {128, 4, true},  {64, 8, false},
+    {128, 8, true},  {256, 4, false}, {256, 8, true},  {128, 16, false}, {512, 4, false},
+    {256, 16, true}, {512, 8, false}, {128, 32, false}, {512, 16, true}, {512, 32, true},
+};
+
+const Cfg *find_cfg(int n, int threads_per_chain) {
+    for (const Cfg &c : kLadder) {
+        if (c.bd * c.ept < n) continue;
+        if (threads_per_chain == 0 ? c.dflt : c.bd == threads_per_chain) return &c;
+    }
+    return nullptr;
+}
+
+}  // namespace
+
+int chain_padded_length(int n, int threads_per_chain) {
+    const Cfg *c = find_cfg(n, threads_per_chain);
+    return c ? c->bd * c->ept : 0;
+}
+
+int chain_block_size(int n, int threads_per_chain) {
+    const Cfg *c = find_cfg(n, threads_per_chain);
+    return c ? c->bd : 0;
+}
+
+int chain_alloc_length(int n) {
+    const int np = chain_padded_length(n, 0);
+    if (np == 0) return 0;
+    return np * 2 > 16384 ? np : np * 2;
+}
+
+int chain_candidates(int n, int max_np, int *bds, int cap) {
+    const int np0 = chain_padded_length(n, 0);
+    int k = 0;
+    for (const Cfg &c : kLadder) {
+        const int np = c.bd * c.ept;
+        if (np < n || np > max_np || (np != np0 && np != 2 * np0)) continue;
+        bool dup = false;
+        for (int j = 0; j < k; ++j) dup |= bds[j] == c.bd;
+        if (dup || chain_padded_length(n, c.bd) != np) continue;
+        if (k < cap) bds[k++] = c.bd;
+    }
+    return k;
+}
+
+size_t chain_smem_bytes(int n, int d, int ldw, int block) {
+    (void)ldw;
+    (void)d;
+    const int np = chain_padded_length(n, block);
+    return sizeof(double) * 3 * (size_t)np + 24 * 64 + 2 * 1792 + 128;
+}
+
+cudaError_t launch_chains(const ChainArgs &a, int threads_per_chain, cudaStream_t stream, int max_ctas,
+                          int *per_sm) {
+    const Cfg *c = find_cfg(a.n, threads_per_chain);
+    if (!c || c->bd * c->ept > a.np) return cudaErrorInvalidValue;
+    if (a.P <= 0 && !per_sm) return cudaSuccess;
+    return c->bd <= 128 ? launch_chain_cfg_small(c->bd, c->ept, a, stream, max_ctas, per_sm)
+                        : launch_chain_cfg_large(c->bd, c->ept, a, stream, max_ctas, per_sm);
+}
+
+}  // namespace achr

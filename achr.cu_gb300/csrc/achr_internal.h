@@ -27,7 +27,7 @@ enum DeviceError : unsigned long long {
 // Everything one chain-sampling launch reads (device pointers) and its scalars.
 struct ChainArgs {
     int n, m, W, d;
-    int np;                     // padded length of the per-element arrays (block size x elements per thread)
+    int np;                     // length the per-element arrays are padded to (>= block size x elements per thread)
     int ldw;                    // leading dimension of the warmup matrix in doubles (even)
     int P, T;
     const double *warmup;       // ldw x W, column j = warmup point j
@@ -51,13 +51,22 @@ struct ChainArgs {
     unsigned long long *counters;  // CNT_SLOTS entries
 };
 
-// Launch the persistent chain kernel; threads_per_chain = 0 picks by size.
-cudaError_t launch_chains(const ChainArgs &a, int threads_per_chain, cudaStream_t stream);
+// Launch the persistent chain kernel; threads_per_chain = 0 picks the default
+// configuration for n.  max_ctas > 0 caps the grid; per_sm (if non-NULL)
+// receives the resident CTAs per SM of the configuration.  a.np is the length
+// the per-reaction arrays were padded to (>= the configuration's BD * EPT).
+cudaError_t launch_chains(const ChainArgs &a, int threads_per_chain, cudaStream_t stream, int max_ctas = 0,
+                          int *per_sm = nullptr);
 
-// Block size and padded element count the launcher uses for n reactions
-// (threads_per_chain = 0 picks by size); 0 if no configuration fits.
+// Configuration ladder: threads per chain and padded element count for n
+// reactions (threads_per_chain = 0: default); 0 if no configuration fits.
 int chain_block_size(int n, int threads_per_chain);
 int chain_padded_length(int n, int threads_per_chain);
+// Length to pad per-reaction arrays to: twice the default padded length (so
+// every autotuning candidate fits), at most 16384.
+int chain_alloc_length(int n);
+// Threads-per-chain values worth timing for n (padded length within max_np).
+int chain_candidates(int n, int max_np, int *bds, int cap);
 size_t chain_smem_bytes(int n, int d, int ldw, int block);
 
 }  // namespace achr

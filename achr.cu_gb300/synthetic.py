@@ -143,7 +143,7 @@ def interior_point(S, lb, ub, cap=50.0):
     return v0, blocked
 
 
-def interior_chord_warmup(S, lb, ub, n_pts, seed=0, null_space=None):
+def interior_chord_warmup(S, lb, ub, n_pts, seed=0, null_space=None, interior=None):
     """Warmup points for genome-scale models (stand-in for createWarmupPtsGLPK).
 
     The reference generates one LP solution per warmup point (FVA extremes,
@@ -155,12 +155,13 @@ def interior_chord_warmup(S, lb, ub, n_pts, seed=0, null_space=None):
     far and near end as the reference alternates max and min; clip, and shrink
     toward the mean with 0.33 x + 0.67 centre (createWarmupPtsGLPK.c:283-284).
     The points satisfy S w = 0 to FP64 rounding.  null_space(S_F) -> basis
-    may be supplied; the default uses numpy's symmetric eigensolver.
+    may be supplied; the default uses numpy's symmetric eigensolver.  interior
+    = (v0, blocked) from interior_point() may be supplied to skip the LP.
     """
     S = np.asarray(S.todense() if hasattr(S, "todense") else S, dtype=np.float64)
     lb = np.asarray(lb, dtype=np.float64)
     ub = np.asarray(ub, dtype=np.float64)
-    v0, blocked = interior_point(S, lb, ub)
+    v0, blocked = interior if interior is not None else interior_point(S, lb, ub)
     free = np.flatnonzero(~blocked)
     SF = S[:, free]
     if null_space is None:
@@ -191,6 +192,21 @@ def interior_chord_warmup(S, lb, ub, n_pts, seed=0, null_space=None):
     pts = np.minimum(np.maximum(pts, lb[:, None]), ub[:, None])
     centre = pts.mean(axis=1)
     return pts * 0.33 + 0.67 * centre[:, None]
+
+
+def batch_spec(k: int, n: int) -> SyntheticSpec:
+    """Model k of the 64-model batch workload: n reactions, 0.7 n metabolites."""
+    return SyntheticSpec(n_rxns=n, n_mets=max(2, int(round(0.7 * n))), irreversible_frac=0.3,
+                         n_exchange=max(2, n // 25), exchange_bound=20.0, seed=1000 + k)
+
+
+def batch_interior(args):
+    """(k, n) -> (k, v0, blocked) for the batch workload; runs in a worker process."""
+    k, n = args
+    spec = batch_spec(k, n)
+    row, col, val, lb, ub = make_model(spec)
+    v0, blocked = interior_point(dense(spec.n_mets, n, row, col, val), lb, ub)
+    return k, v0, blocked
 
 
 def ideal_bytes_per_chain_step(n: int) -> int:

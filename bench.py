@@ -47,7 +47,7 @@ def parse_args():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="genome")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["batch64"], default="genome")
     ap.add_argument("--seed", type=int, default=20261203)
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target length of the CPU baseline sample")
     ap.add_argument("--no-e2e", action="store_true")
@@ -352,8 +352,112 @@ def run_profile_case(args):
     return 0
 
 
+def _batch_interior_worker(job):
+    """LP interior point of one batch model, in a spawned worker process."""
+    import importlib
+
+    import __graft_entry__ as ge
+
+    ge.load_package()
+    return importlib.import_module("achr_gb300.synthetic").batch_interior(job)
+
+
+def run_batch(args):
+    """64 synthetic models of uneven size sampled in one CUDA-graph launch.
+
+    Reaction counts log-uniform in [95, 7440], metabolites 0.7 n, the same S and
+    bound law, warmup 2n per model, chains per model proportional to n summing
+    to 262,144, 1000 steps; each model's chain-kernel configuration comes from
+    the autotuner.  Prints one JSON line (not the driver's headline metric)."""
+    import torch
+
+    import __graft_entry__ as ge
+
+    pkg = ge.load_package()
+    import importlib
+    synth = importlib.import_module("achr_gb300.synthetic")
+    sizes = synth.log_uniform_sizes(64, 95, 7440, seed=64)
+    chains_total, T = 262_144, 1000
+    weights = np.array(sizes, dtype=np.float64)
+    P = np.floor(chains_total * weights / weights.sum()).astype(int)
+    P[np.argmax(P)] += chains_total - int(P.sum())
+
+    t_setup = time.perf_counter()
+    # interior points by LP in a worker pool (CPU only; spawned before any GPU use)
+    interiors = {}
+    todo = [(k, n) for k, n in enumerate(sizes)
+            if not (Path("/tmp") / f"achr_batch_{n}_{1000 + k}_v1.npz").exists()]
+    if todo:
+        import multiprocessing as mp
+        with mp.get_context("spawn").Pool(min(len(todo), os.cpu_count() or 1)) as pool:
+            for k, v0, blocked in pool.imap_unordered(_batch_interior_worker, sorted(todo, key=lambda t: -t[1])):
+                interiors[k] = (v0, blocked)
+    pkg.lib()
+
+    def gpu_null_space(SF):
+        r, c = np.nonzero(SF)
+        m = pkg.HostModel(SF.shape[1], SF.shape[0], r, c, SF[r, c], np.full(SF.shape[1], -1.0),
+                          np.full(SF.shape[1], 1.0))
+        with pkg.Sampler(m, np.zeros((SF.shape[1], 1))) as tmp:
+            return tmp.null_space()
+
+    samplers, outs = [], []
+    for k, n in enumerate(sizes):
+        spec = synth.batch_spec(k, n)
+        cache = Path("/tmp") / f"achr_batch_{n}_{spec.seed}_v1.npz"
+        row, col, val, lb, ub = synth.make_model(spec)
+        if cache.exists():
+            warm = np.load(cache)["warm"]
+        else:
+            S = synth.dense(spec.n_mets, spec.n_rxns, row, col, val)
+            warm = synth.interior_chord_warmup(S, lb, ub, 2 * n, seed=spec.seed, null_space=gpu_null_space,
+                                               interior=interiors[k])
+            np.savez(cache, warm=warm)
+        s = pkg.Sampler(pkg.HostModel(n, spec.n_mets, row, col, val, lb, ub), warm)
+        s.autotune()
+        samplers.append(s)
+        outs.append(torch.empty((n, int(P[k])), dtype=torch.float64, device="cuda"))
+    batch_setup_s = time.perf_counter() - t_setup
+    stream = torch.cuda.current_stream().cuda_stream
+    ptrs = [o.data_ptr() for o in outs]
+    counts = [int(p) for p in P]
+    for w in range(args.warmup):
+        pkg.sample_batch(samplers, counts, min(T, 50), ptrs, counts, stream=stream, seed=args.seed + w)
+    clocks = ClockSampler(0)
+    clocks.start()
+    runs = []
+    for k in range(args.steps):
+        runs.append(pkg.sample_batch(samplers, counts, T, ptrs, counts, stream=stream, seed=args.seed + 100 + k))
+    clk = clocks.stop()
+    graph_ms = sum(r[0]["graph_ms"] for r in runs) / len(runs)
+    chain_steps = int(P.sum()) * T
+    alg = sum(synth.ideal_bytes_per_chain_step(n) * int(p) * T for n, p in zip(sizes, P))
+    peak, peak_kind = load_peaks()
+    line = {
+        "metric": METRIC, "value": chain_steps / (graph_ms * 1e-3), "unit": METRIC, "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": graph_ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"batch64: 64 synthetic models, n log-uniform in [95, 7440] (sum {sum(sizes)}), "
+                               f"{int(P.sum())} chains in total (proportional to n) x {T} steps, one CUDA-graph launch",
+                   "threads_per_chain": sorted({s.options.threads_per_chain for s in samplers})},
+        "load_imbalance": sum(r[0]["load_imbalance"] for r in runs) / len(runs),
+        "roofline": {"bound": "hbm", "achieved": alg / (graph_ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
+                     "frac": alg / (graph_ms * 1e-3) / 1e9 / peak, "traffic": None,
+                     "peak_source": f"{peak_kind} hbm_gbs"},
+        "clocks": clk, "setup_s": batch_setup_s,
+        "sampler": {k: runs[-1][0][k] for k in ("accepted", "rejected", "reprojections", "stuck_chains",
+                                                 "max_residual", "max_bound_violation")},
+    }
+    print(json.dumps(line), flush=True)
+    for s in samplers:
+        s.close()
+    return 0
+
+
 def main():
     args = parse_args()
+    if args.workload == "batch64":
+        return run_batch(args)
     if args.profile_case:
         return run_profile_case(args)
     if args.impl == "reference":

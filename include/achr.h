@@ -140,6 +140,34 @@ achr_status achr_sample_device(achr_ctx *ctx, uint64_t seed, uint64_t chain_offs
 /* Release every device and host resource of the context. */
 void achr_destroy(achr_ctx *ctx);
 
+/* ---- Tuning and batched sampling (no counterpart in the reference, which
+ * hard-codes 8-thread blocks, ACHRCuda.cu:715, and runs one model per process) ---- */
+
+/* Time the chain kernel's candidate configurations (threads per chain x
+ * reactions per thread) on a short run of this context and keep the fastest in
+ * its options; the choice is cached per padded model size and device for the
+ * rest of the process.  Writes the chosen threads per chain if non-NULL. */
+achr_status achr_autotune(achr_ctx *ctx, int32_t *threads_per_chain_out);
+
+typedef struct {
+    double graph_ms;            /* device time of the whole batched launch */
+    double load_imbalance;      /* (max - mean) / max over the models' finish times */
+    int64_t accepted, rejected, reprojections, stuck_chains;
+    double max_residual, max_bound_violation;
+} achr_batch_stats;
+
+/* Sample several models at once: one CUDA graph launch holding one persistent
+ * chain kernel per model on its own stream, each given a share of the SMs in
+ * proportion to its work (chains x steps x padded reactions).  Model k runs
+ * n_points[k] chains of n_steps into d_points_out[k] (device, n_k x P_k,
+ * leading dimension ld_out[k]); its chain ids start at the sum of the earlier
+ * models' n_points, so achr_sample_device on model k alone with that
+ * chain_offset gives the same points.  Synchronises `stream`; per-model finish
+ * times (ms from the launch) go to model_ms_out[k] if non-NULL. */
+achr_status achr_sample_batch(achr_ctx *const *ctxs, int32_t n_models, const int32_t *n_points, int32_t n_steps,
+                              uint64_t seed, double *const *d_points_out, const int64_t *ld_out, void *stream,
+                              achr_batch_stats *stats, double *model_ms_out);
+
 /* ---- Sampling without any allocation ---- */
 
 /* Largest model (reactions) achr_sample_noalloc accepts: its working data sits
