@@ -116,6 +116,8 @@ _SIGNATURES = {
     "achr_sample_device": (C.c_int, [C.c_void_p, C.c_uint64, C.c_uint64, C.c_int32, C.c_int32, C.c_void_p,
                                      C.c_int64, C.c_void_p, C.POINTER(Stats)]),
     "achr_destroy": (None, [C.c_void_p]),
+    "achr_sample_resume": (C.c_int, [C.c_void_p, C.c_uint64, C.c_uint64, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
+                                     C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.POINTER(Stats)]),
     "achr_autotune": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
     "achr_sample_batch": (C.c_int, [C.POINTER(C.c_void_p), C.c_int32, C.POINTER(C.c_int32), C.c_int32, C.c_uint64,
                                     C.POINTER(C.c_void_p), C.POINTER(C.c_int64), C.c_void_p, C.POINTER(BatchStats),
@@ -327,6 +329,16 @@ class Sampler:
         st = Stats()
         _check(lib().achr_sample(self._ctx, seed, chain_offset, n_points, n_steps, _dptr(out), C.byref(st)))
         return out, st.as_dict()
+
+    def sample_resume(self, n_points: int, step0: int, n_steps: int, resume: bool, d_points: int, d_centre_acc: int,
+                      ld: int, stream: int = 0, seed: int = 0, chain_offset: int = 0,
+                      with_stats: bool = False) -> Optional[dict]:
+        """Start or continue chains in place on device state buffers (achr_sample_resume)."""
+        st = Stats() if with_stats else None
+        _check(lib().achr_sample_resume(self._ctx, seed, chain_offset, n_points, step0, n_steps, int(resume),
+                                        C.c_void_p(d_points), C.c_void_p(d_centre_acc), ld, C.c_void_p(stream),
+                                        C.byref(st) if st is not None else None))
+        return st.as_dict() if st is not None else None
 
     def autotune(self) -> int:
         """Pick the fastest chain-kernel configuration for this model; returns threads per chain."""

@@ -121,6 +121,7 @@ __global__ void centre_kernel(int n, int W, int ldw, const double *__restrict__ 
 struct achr_ctx {
     int n = 0, m = 0, W = 0, d = 0, ldw = 0, np = 0;
     float bound_err = 0.0f;
+    double tuned_rate = 0.0;  // chain-steps per ms on the whole GPU with the tuned configuration (0: not measured)
     int device = 0;
     achr_options opt{};
     std::vector<double> h_lb, h_ub;
@@ -613,12 +614,56 @@ ChainArgs chain_args(const achr_ctx *ctx, uint64_t seed, uint64_t chain_offset, 
     a.d_tol = ctx->opt.d_tol;
     a.feasibility_tol = ctx->opt.feasibility_tol;
     a.counters = ctx->counters.p;
+    a.step0 = 0;
+    a.x_in = nullptr;
+    a.A_in = nullptr;
+    a.A_out = nullptr;
+    a.ld_state = 0;
     return a;
 }
 
 }  // namespace
 
 extern "C" {
+
+achr_status achr_sample_resume(achr_ctx *ctx, uint64_t seed, uint64_t chain_offset, int32_t n_points, int32_t step0,
+                               int32_t n_steps, int32_t resume, double *d_points, double *d_centre_acc, int64_t ld,
+                               void *stream, achr_stats *stats) {
+    if (!ctx) return fail(ACHR_ERR_INVALID, "ctx is NULL");
+    if (n_points < 0 || n_steps < 0 || step0 < 0 || (!resume && step0 != 0))
+        return fail(ACHR_ERR_INVALID, "bad step range (a fresh start begins at step 0)");
+    if ((int64_t)step0 + n_steps > 2147483647LL) return fail(ACHR_ERR_INVALID, "step index overflow");
+    if (n_points > 0 && (!d_points || !d_centre_acc || ld < n_points))
+        return fail(ACHR_ERR_INVALID, "bad state buffers");
+    cudaStream_t s = (cudaStream_t)stream;
+    ChainArgs a = chain_args(ctx, seed, chain_offset, n_points, n_steps, d_points, ld);
+    a.step0 = step0;
+    a.x_in = resume ? d_points : nullptr;
+    a.A_in = resume ? d_centre_acc : nullptr;
+    a.A_out = d_centre_acc;
+    a.ld_state = ld;
+    ACHR_CUDA_TRY(cudaMemsetAsync(ctx->counters.p, 0, sizeof(unsigned long long) * achr::CNT_SLOTS, s));
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (stats) {
+        ACHR_CUDA_TRY(cudaEventCreate(&e0));
+        ACHR_CUDA_TRY(cudaEventCreate(&e1));
+        ACHR_CUDA_TRY(cudaEventRecord(e0, s));
+    }
+    cudaError_t e = achr::launch_chains(a, ctx->opt.threads_per_chain, s);
+    if (e != cudaSuccess) {
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+        return cuda_fail(e, "chain kernel launch");
+    }
+    if (!stats) return ACHR_OK;
+    ACHR_CUDA_TRY(cudaEventRecord(e1, s));
+    ACHR_CUDA_TRY(cudaEventSynchronize(e1));
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return read_counters(ctx, stats, ms);
+}
 
 achr_status achr_sample(achr_ctx *ctx, uint64_t seed, uint64_t chain_offset, int32_t n_points, int32_t n_steps,
                         double *points_out, achr_stats *stats) {
@@ -663,17 +708,17 @@ achr_status achr_autotune(achr_ctx *ctx, int32_t *threads_per_chain_out) {
     int dev = 0;
     ACHR_CUDA_TRY(cudaGetDevice(&dev));
     const std::pair<int, int> key(achr::chain_padded_length(ctx->n, 0), dev);
+    int cand[8];
+    int nc = 0;
     {
         std::lock_guard<std::mutex> lock(g_tune_mutex);
         auto it = g_tune_cache.find(key);
-        if (it != g_tune_cache.end()) {
-            ctx->opt.threads_per_chain = it->second;
-            if (threads_per_chain_out) *threads_per_chain_out = it->second;
-            return ACHR_OK;
+        if (it != g_tune_cache.end()) {  // known size: time only the cached choice (its rate feeds batching)
+            cand[0] = it->second;
+            nc = 1;
         }
     }
-    int cand[8];
-    const int nc = achr::chain_candidates(ctx->n, ctx->np, cand, 8);
+    if (nc == 0) nc = achr::chain_candidates(ctx->n, ctx->np, cand, 8);
     if (nc == 0) return fail(ACHR_ERR_UNSUPPORTED, "no chain-kernel configuration to tune");
     int sms = 0;
     ACHR_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
@@ -699,6 +744,7 @@ achr_status achr_autotune(achr_ctx *ctx, int32_t *threads_per_chain_out) {
         }
     }
     ctx->opt.threads_per_chain = best;
+    ctx->tuned_rate = best_ms > 0 ? (double)P * T / best_ms : 0.0;
     {
         std::lock_guard<std::mutex> lock(g_tune_mutex);
         g_tune_cache[key] = best;
@@ -715,7 +761,7 @@ achr_status achr_sample_batch(achr_ctx *const *ctxs, int32_t n_models, const int
     int dev = 0, sms = 0;
     ACHR_CUDA_TRY(cudaGetDevice(&dev));
     ACHR_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    // Work of each model (padded elements x chain-steps) sets its share of the SMs.
+    // Predicted time of each model orders the launches.
     std::vector<double> work((size_t)n_models);
     std::vector<int> per_sm((size_t)n_models);
     std::vector<uint64_t> offset((size_t)n_models);
@@ -728,8 +774,11 @@ achr_status achr_sample_batch(achr_ctx *const *ctxs, int32_t n_models, const int
         const ChainArgs a0 = chain_args(c, seed, 0, 0, n_steps, d_points_out[k], ld_out[k]);
         cudaError_t e = achr::launch_chains(a0, c->opt.threads_per_chain, nullptr, 0, &per_sm[(size_t)k]);
         if (e != cudaSuccess) return cuda_fail(e, "chain kernel configuration");
-        work[(size_t)k] = (double)n_points[k] * (double)n_steps *
-                          (double)achr::chain_padded_length(c->n, c->opt.threads_per_chain);
+        // predicted time on the whole GPU: measured by the autotuner, else padded elements x chain-steps
+        work[(size_t)k] = c->tuned_rate > 0
+                              ? (double)n_points[k] * (double)n_steps / c->tuned_rate
+                              : (double)n_points[k] * (double)n_steps *
+                                    (double)achr::chain_padded_length(c->n, c->opt.threads_per_chain) * 1e-9;
         total += work[(size_t)k];
         offset[(size_t)k] = off;  // disjoint chain ids: model k uses ids off .. off + P_k - 1
         off += (uint64_t)n_points[k];
@@ -759,16 +808,20 @@ achr_status achr_sample_batch(achr_ctx *const *ctxs, int32_t n_models, const int
     stamp_kernel<<<1, 1, 0, main>>>(stamps.p + n_models);
     cudaError_t ce = cudaGetLastError();
     if (ce == cudaSuccess) ce = cudaEventRecord(fork, main);
-    for (int k = 0; k < n_models && ce == cudaSuccess; ++k) {
+    // Longest predicted model first; one CTA per chain, so the CTA scheduler
+    // hands every SM slot that frees up to whichever model still has chains.
+    std::vector<int> order((size_t)n_models);
+    for (int k = 0; k < n_models; ++k) order[(size_t)k] = k;
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return work[(size_t)x] > work[(size_t)y]; });
+    for (int q = 0; q < n_models && ce == cudaSuccess; ++q) {
+        const int k = order[(size_t)q];
         cudaStream_t sk = ss.streams[first + (size_t)k];
         achr_ctx *c = ctxs[k];
         ce = cudaStreamWaitEvent(sk, fork, 0);
         if (ce == cudaSuccess)
             ce = cudaMemsetAsync(c->counters.p, 0, sizeof(unsigned long long) * achr::CNT_SLOTS, sk);
-        const double share = total > 0 ? work[(size_t)k] / total : 1.0 / n_models;
-        const int sm_share = std::max(1, (int)std::lround(share * sms));
         const ChainArgs a = chain_args(c, seed, offset[(size_t)k], n_points[k], n_steps, d_points_out[k], ld_out[k]);
-        if (ce == cudaSuccess) ce = achr::launch_chains(a, c->opt.threads_per_chain, sk, sm_share * per_sm[(size_t)k]);
+        if (ce == cudaSuccess) ce = achr::launch_chains(a, c->opt.threads_per_chain, sk, -1);
         if (ce == cudaSuccess) {
             stamp_kernel<<<1, 1, 0, sk>>>(stamps.p + k);
             ce = cudaGetLastError();

@@ -303,25 +303,36 @@ __global__ void __launch_bounds__(BD, (BD <= 256 ? 2 : 1)) achr_chain_kernel(con
 
     for (long long p = blockIdx.x; p < a.P && !failed; p += gridDim.x) {
         const unsigned long long chain = a.chain_offset + (unsigned long long)p;
+        if (a.x_in) {  // resume: the chain's point and centre accumulator after step0 steps
 #pragma unroll
-        for (int k = 0; k < EPT; ++k) {
-            const int i = tid + k * BD;
-            xs[i] = a.c0[i];
-            As[i] = a.A0[i];
+            for (int k = 0; k < EPT; ++k) {
+                const int i = tid + k * BD;
+                const bool real = i < a.n;
+                xs[i] = real ? a.x_in[(size_t)i * (size_t)a.ld_state + (size_t)p] : 0.0;
+                As[i] = real ? a.A_in[(size_t)i * (size_t)a.ld_state + (size_t)p] : 0.0;
+            }
+        } else {
+#pragma unroll
+            for (int k = 0; k < EPT; ++k) {
+                const int i = tid + k * BD;
+                xs[i] = a.c0[i];
+                As[i] = a.A0[i];
+            }
         }
         long long buf_col = -1;
-        bool inflight = false, any_accepted = false, stuck = false;
-        int chk = 0;  // accepted steps since the last residual check (ACHRCuda.cu:325)
-        int tbase = -kTbl;
+        bool inflight = false, any_accepted = a.x_in != nullptr, stuck = false;
+        const int s_end = a.step0 + a.T;
+        int chk = a.step0 % a.check_period;  // the reference checks when the step count is a multiple (ACHRCuda.cu:325)
+        int tbase = a.step0 - kTbl;
 
-        for (int s = 0; s < a.T && !stuck && !failed; ++s) {
+        for (int s = a.step0; s < s_end && !stuck && !failed; ++s) {
             if (s - tbase >= kTbl) {
                 // refill the step table: entry e holds step tbase + e
                 tbase = s;
                 __syncthreads();
                 for (int e = tid; e < kTbl; e += BD) {
                     const int st = s + e;
-                    if (st < a.T) {
+                    if (st < s_end) {
                         const Philox4 pd = step_draw(a.seed, chain, (uint32_t)st, 0u);
                         StepEntry en;
                         en.U = step_uniform(pd);
@@ -403,7 +414,7 @@ __global__ void __launch_bounds__(BD, (BD <= 256 ? 2 : 1)) achr_chain_kernel(con
                 const float norm32 = sqrtf(ss);
 
                 // Prefetch the next step's warmup column while this one is tested.
-                if (s + 1 < a.T) {
+                if (s + 1 < s_end) {
                     const long long rn =
                         (s + 1 - tbase < kTbl)
                             ? (long long)tbl[s + 1 - tbase].idx
@@ -771,6 +782,8 @@ __global__ void __launch_bounds__(BD, (BD <= 256 ? 2 : 1)) achr_chain_kernel(con
             worst_viol = fmax(worst_viol, __longlong_as_double((long long)vb));
         }
         for (int i = tid; i < a.n; i += BD) a.out[(size_t)i * (size_t)a.ld_out + (size_t)p] = any_accepted ? xs[i] : 0.0;
+        if (a.A_out)
+            for (int i = tid; i < a.n; i += BD) a.A_out[(size_t)i * (size_t)a.ld_state + (size_t)p] = As[i];
         __syncthreads();
     }
 
@@ -788,7 +801,8 @@ __global__ void __launch_bounds__(BD, (BD <= 256 ? 2 : 1)) achr_chain_kernel(con
 }
 
 // Occupancy-sized persistent launch of one configuration.  max_ctas > 0 caps
-// the grid (batched launches share the SMs between models).
+// the grid; max_ctas < 0 launches one CTA per chain, leaving the balancing of
+// concurrent launches to the hardware CTA scheduler (batched models).
 template <int BD, int EPT>
 cudaError_t launch_cfg(const ChainArgs &a, cudaStream_t stream, int max_ctas, int *per_sm_out) {
     const size_t smem = chain_smem_bytes_cfg(BD * EPT, a.d, BD);
@@ -804,7 +818,7 @@ cudaError_t launch_cfg(const ChainArgs &a, cudaStream_t stream, int max_ctas, in
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    long long grid = (long long)sms * per_sm;
+    long long grid = max_ctas < 0 ? (long long)a.P : (long long)sms * per_sm;
     if (max_ctas > 0 && grid > max_ctas) grid = max_ctas;
     if (grid > a.P) grid = a.P;
     if (grid < 1) return cudaSuccess;

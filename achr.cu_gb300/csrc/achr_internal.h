@@ -44,6 +44,11 @@ struct ChainArgs {
     const double *N;            // n x d column-major null-space basis (ld = n)
     double *out;                // n x P row-major block: out[i * ld_out + p]
     long long ld_out;
+    int step0;                  // global index of the first step of this launch (resumed chains)
+    const double *x_in;         // NULL: chains start at the centre; else n x P points to resume from (ld_state)
+    const double *A_in;         // with x_in: n x P centre accumulators (W + step0 + offset) c
+    double *A_out;              // NULL or n x P: centre accumulators after the last step (ld_state)
+    long long ld_state;
     unsigned long long seed, chain_offset;
     int check_period, max_attempts, centre_offset, exact_ratio;
     int final_project;          // 1: project+clip emitted points whose residual exceeds feasibility_tol

@@ -224,6 +224,11 @@ extern "C" achr_status achr_sample_noalloc(const achr_device_model *m, const ach
     a.d_tol = opt.d_tol;
     a.feasibility_tol = opt.feasibility_tol;
     a.counters = sv.counters;
+    a.step0 = 0;
+    a.x_in = nullptr;
+    a.A_in = nullptr;
+    a.A_out = nullptr;
+    a.ld_state = 0;
     cudaError_t e = achr::launch_chains(a, opt.threads_per_chain, s);
     if (e != cudaSuccess) return fail(ACHR_ERR_CUDA, std::string("chain kernel launch: ") + cudaGetErrorString(e));
     if (!stats) return ACHR_OK;

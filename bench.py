@@ -52,6 +52,9 @@ def parse_args():
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target length of the CPU baseline sample")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--ess", type=int, nargs=4, metavar=("CHAINS", "BURNIN", "SEGMENTS", "STEPS"),
+                    help="min-ESS/s and max R-hat from trace snapshots: CHAINS chains, BURNIN steps, then SEGMENTS "
+                         "snapshots STEPS steps apart")
     ap.add_argument("--profile-case", type=int, nargs=2, metavar=("CHAINS", "STEPS"),
                     help="run two launches of CHAINS x STEPS of the workload and print their times (ncu captures)")
     return ap.parse_args()
@@ -441,6 +444,7 @@ def run_batch(args):
                                f"{int(P.sum())} chains in total (proportional to n) x {T} steps, one CUDA-graph launch",
                    "threads_per_chain": sorted({s.options.threads_per_chain for s in samplers})},
         "load_imbalance": sum(r[0]["load_imbalance"] for r in runs) / len(runs),
+        "model_finish_ms": {"min": min(runs[-1][1]), "median": float(np.median(runs[-1][1])), "max": max(runs[-1][1])},
         "roofline": {"bound": "hbm", "achieved": alg / (graph_ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
                      "frac": alg / (graph_ms * 1e-3) / 1e9 / peak, "traffic": None,
                      "peak_source": f"{peak_kind} hbm_gbs"},
@@ -454,8 +458,65 @@ def run_batch(args):
     return 0
 
 
+def run_ess(args):
+    """min over fluxes of bulk ESS per second of sampling, and max split-R-hat.
+
+    Chains run BURNIN steps from the warmup centre, then SEGMENTS launches of
+    STEPS steps each (achr_sample_resume); the points after every segment are
+    the draws.  The time is the device time of all launches (burn-in included);
+    the trace copies and the diagnostics are not timed."""
+    import torch
+
+    import __graft_entry__ as ge
+
+    pkg = ge.load_package()
+    pkg.lib()
+    import importlib
+    synth = importlib.import_module("achr_gb300.synthetic")
+    diag = importlib.import_module("achr_gb300.diagnostics")
+    spec, model, S, warm, _, _ = build_inputs(args.workload, pkg, synth)
+    M, B, K, L = args.ess
+    n = spec.n_rxns
+    smp = pkg.Sampler(model, warm)
+    pts = torch.zeros((n, M), dtype=torch.float64, device="cuda")
+    acc = torch.zeros((n, M), dtype=torch.float64, device="cuda")
+    trace = torch.empty((K, n, M), dtype=torch.float64, device="cuda")
+    stream = torch.cuda.current_stream().cuda_stream
+    ms = 0.0
+    st = smp.sample_resume(M, 0, B, False, pts.data_ptr(), acc.data_ptr(), M, stream=stream, seed=args.seed,
+                           with_stats=True)
+    ms += st["kernel_ms"]
+    acc_steps = st["accepted"]
+    for k in range(K):
+        st = smp.sample_resume(M, B + k * L, L, True, pts.data_ptr(), acc.data_ptr(), M, stream=stream,
+                               seed=args.seed, with_stats=True)
+        ms += st["kernel_ms"]
+        acc_steps += st["accepted"]
+        trace[k].copy_(pts)
+    torch.cuda.synchronize()
+    draws = trace.permute(2, 0, 1).cpu().numpy()  # (chains, draws, fluxes)
+    t0 = time.perf_counter()
+    summ = diag.summarize(draws)
+    diag_s = time.perf_counter() - t0
+    line = {
+        "metric": "min-ESS/s", "value": summ["min_ess"] / (ms * 1e-3), "unit": "effective samples/s",
+        "higher_is_better": True, "n_gpus": 1, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"{args.workload}: {spec.n_mets}x{n}, {M} chains, {B} burn-in steps, {K} draws "
+                               f"{L} steps apart, plain ACHR (reference semantics)"},
+        "max_rhat": summ["max_rhat"], "rhat_below_1.01": summ["max_rhat"] < 1.01, "min_ess": summ["min_ess"],
+        "median_rhat": summ["median_rhat"], "rhat_q99": summ["rhat_q99"], "median_ess": summ["median_ess"],
+        "fluxes": summ["params"], "frozen_fluxes": summ["frozen_params"], "sampling_ms": ms,
+        "chain_steps_per_s": acc_steps / (ms * 1e-3), "diagnostics_s": diag_s,
+    }
+    print(json.dumps(line), flush=True)
+    smp.close()
+    return 0
+
+
 def main():
     args = parse_args()
+    if args.ess:
+        return run_ess(args)
     if args.workload == "batch64":
         return run_batch(args)
     if args.profile_case:

@@ -137,6 +137,21 @@ achr_status achr_sample_device(achr_ctx *ctx, uint64_t seed, uint64_t chain_offs
                                int32_t n_steps, double *d_points_out, int64_t ld_out, void *stream,
                                achr_stats *stats);
 
+/* Start (resume = 0) or continue (resume = 1) chains in segments: the
+ * checkpoint/resume the reference lacks (its MATLAB counterpart keeps the last
+ * point, ACHRSamplerMOD.m:176-183).  d_points and d_centre_acc are device
+ * buffers n x P row-major (leading dimension ld): the chains' points and
+ * their centre accumulators (W + t + centre_offset) * centre after step t.
+ * A fresh start begins at step0 = 0 and writes both; a resumed launch reads
+ * both as the state after step0 steps and overwrites them with the state
+ * after step0 + n_steps.  Running T1 then T2 steps this way gives the same
+ * points as one launch of T1 + T2 steps (the random stream is keyed by the
+ * global step index), except in ACHR_MODE_FEASIBLE, where every segment ends
+ * with the feasibility projection.  Queued on `stream`; stats synchronise. */
+achr_status achr_sample_resume(achr_ctx *ctx, uint64_t seed, uint64_t chain_offset, int32_t n_points, int32_t step0,
+                               int32_t n_steps, int32_t resume, double *d_points, double *d_centre_acc, int64_t ld,
+                               void *stream, achr_stats *stats);
+
 /* Release every device and host resource of the context. */
 void achr_destroy(achr_ctx *ctx);
 
@@ -156,9 +171,11 @@ typedef struct {
     double max_residual, max_bound_violation;
 } achr_batch_stats;
 
-/* Sample several models at once: one CUDA graph launch holding one persistent
- * chain kernel per model on its own stream, each given a share of the SMs in
- * proportion to its work (chains x steps x padded reactions).  Model k runs
+/* Sample several models at once: one CUDA graph launch holding one chain
+ * kernel per model, each on its own stream, one CTA per chain, launched in
+ * order of predicted time (from the throughput achr_autotune measured for the
+ * model, else chains x steps x padded reactions) so that the hardware CTA
+ * scheduler keeps every SM busy until the last chains finish.  Model k runs
  * n_points[k] chains of n_steps into d_points_out[k] (device, n_k x P_k,
  * leading dimension ld_out[k]); its chain ids start at the sum of the earlier
  * models' n_points, so achr_sample_device on model k alone with that

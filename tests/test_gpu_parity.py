@@ -182,3 +182,25 @@ def test_gpu_null_space_svd_of_s(pkg, small_model, golden):
     assert N.shape == golden["N"].shape
     assert np.abs(S @ N).max() < 1e-12
     assert np.abs(N @ N.T - golden["N"] @ golden["N"].T).max() < 1e-10
+
+
+def test_resume_in_segments_equals_one_run(sampler):
+    """12 + 9 + 17 steps in three launches give the points of one 38-step launch."""
+    torch = pytest.importorskip("torch")
+    P, n = 48, sampler.n
+    pts = torch.zeros((n, P), dtype=torch.float64, device="cuda")
+    acc = torch.zeros((n, P), dtype=torch.float64, device="cuda")
+    stream = torch.cuda.current_stream().cuda_stream
+    step = 0
+    for seg, resume in ((12, False), (9, True), (17, True)):
+        st = sampler.sample_resume(P, step, seg, resume, pts.data_ptr(), acc.data_ptr(), P, stream=stream, seed=21,
+                                   chain_offset=5, with_stats=True)
+        assert st["accepted"] == P * seg
+        step += seg
+    ref, _ = sampler.sample(P, 38, seed=21, chain_offset=5)
+    assert np.array_equal(pts.cpu().numpy(), ref)
+
+
+def test_resume_rejects_fresh_start_off_zero(sampler, pkg):
+    with pytest.raises(pkg.AchrError):
+        sampler.sample_resume(4, 3, 5, False, 16, 16, 4)
