@@ -141,16 +141,32 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
+def cpu_chains_for(prob, T, seed, target_s, threads):
+    """Chains (a multiple of the thread count) whose T steps take about target_s on the oracle.
+
+    A first short call pays the one-time costs (thread start-up, first touch of the warmup
+    matrix); the probe then doubles its chain count until it runs for at least 0.3 s, so that
+    the per-call overhead does not inflate the estimated cost of a chain-step."""
+    prob.sample(seed, threads, 5, chain_offset=2 * 10**9, threads=threads)
+    steps = min(T, 100)
+    chains = threads
+    while True:
+        t0 = time.perf_counter()
+        prob.sample(seed, chains, steps, chain_offset=10**9, threads=threads)
+        el = time.perf_counter() - t0
+        if el >= 0.3 or chains * steps * 1.0 >= 1e9:
+            break
+        chains *= 2
+    rate = chains * steps / el  # chain-steps per second
+    rounds = max(1, int(target_s * rate / (T * threads)))
+    return threads * rounds
+
+
 def cpu_baseline(oracle, model, warm, N, T, seed, target_s):
     """Time the oracle (all host threads) on a bounded chain sample of the workload."""
     threads = os.cpu_count() or 1
     prob = oracle.Problem(model, warm, N)
-    probe_steps = 50
-    t0 = time.perf_counter()
-    prob.sample(seed, threads, probe_steps, chain_offset=10**9, threads=threads)
-    per_round = (time.perf_counter() - t0) / probe_steps  # seconds per step for `threads` chains
-    rounds = max(1, int(target_s / max(per_round * T, 1e-9)))
-    P = threads * rounds
+    P = cpu_chains_for(prob, T, seed, target_s, threads)
     t0 = time.perf_counter()
     _, st = prob.sample(seed, P, T, threads=threads)
     el = time.perf_counter() - t0
@@ -183,11 +199,7 @@ def run_reference(args):
     threads = os.cpu_count() or 1
     prob = oracle.Problem(model, warm, N)
     # each step: a bounded chain sample of the workload sized to ~8 s
-    t0 = time.perf_counter()
-    prob.sample(args.seed, threads, 50, chain_offset=10**9, threads=threads)
-    per_round = (time.perf_counter() - t0) / 50
-    rounds = max(1, int(8.0 / max(per_round * T, 1e-9)))
-    Pstep = threads * rounds
+    Pstep = min(P, cpu_chains_for(prob, T, args.seed, 8.0, threads))
     for w in range(args.warmup):
         prob.sample(args.seed + w, threads, min(T, 50), threads=threads)
     times, acc = [], 0
