@@ -102,6 +102,17 @@ class BatchStats(C.Structure):
         return {name: getattr(self, name) for name, _ in self._fields_}
 
 
+class ReprojStats(C.Structure):
+    _fields_ = [
+        ("residual_before", C.c_double), ("residual_after", C.c_double), ("gemm_ms", C.c_double),
+        ("total_ms", C.c_double), ("gemm_flops", C.c_double), ("rounds", C.c_int32), ("rank", C.c_int32),
+        ("lambda_min", C.c_double), ("lambda_max", C.c_double),
+    ]
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
 # Every symbol include/achr.h declares, with its ctypes signature.
 _SIGNATURES = {
     "achr_default_options": (None, [C.POINTER(Options)]),
@@ -124,6 +135,13 @@ _SIGNATURES = {
                                     C.POINTER(C.c_double)]),
     "achr_sample_noalloc": (C.c_int, [C.POINTER(DeviceModel), C.POINTER(Options), C.c_uint64, C.c_uint64, C.c_int32,
                                       C.c_int32, C.c_void_p, C.c_int64, C.c_void_p, C.POINTER(Stats)]),
+    "achr_reproject_batch": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_int64, C.c_int32,
+                                       C.c_void_p, C.POINTER(ReprojStats)]),
+    "achr_sample_periodic": (C.c_int, [C.c_void_p, C.c_uint64, C.c_uint64, C.c_int32, C.c_int32, C.c_int32,
+                                       C.c_int32, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.POINTER(Stats),
+                                       C.POINTER(ReprojStats)]),
+    "achr_gemm_bf16": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_int64,
+                                 C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_int64, C.c_void_p]),
     "achr_read_mps": (C.c_int, [C.c_char_p, C.POINTER(ModelBuf)]),
     "achr_free_model": (None, [C.POINTER(ModelBuf)]),
     "achr_read_warmup_csv": (C.c_int, [C.c_char_p, C.c_int32, C.POINTER(C.POINTER(C.c_double)),
@@ -340,6 +358,24 @@ class Sampler:
                                         C.byref(st) if st is not None else None))
         return st.as_dict() if st is not None else None
 
+    def reproject(self, n_points: int, d_points: int, ld: int, d_centre_acc: int = 0, max_rounds: int = 1,
+                  stream: int = 0, with_stats: bool = True) -> Optional[dict]:
+        """Reproject chains 0..P-1 of an n x ld device block in place (achr_reproject_batch)."""
+        st = ReprojStats() if with_stats else None
+        _check(lib().achr_reproject_batch(self._ctx, n_points, C.c_void_p(d_points), C.c_void_p(d_centre_acc or None),
+                                          ld, max_rounds, C.c_void_p(stream), C.byref(st) if st is not None else None))
+        return st.as_dict() if st is not None else None
+
+    def sample_periodic(self, n_points: int, n_steps: int, period: int, d_points: int, d_centre_acc: int, ld: int,
+                        stream: int = 0, seed: int = 0, chain_offset: int = 0, max_rounds: int = 4):
+        """T steps in segments of `period`, each followed by a batched reprojection
+        (achr_sample_periodic).  Returns (sampling stats, reprojection stats)."""
+        st, rs = Stats(), ReprojStats()
+        _check(lib().achr_sample_periodic(self._ctx, seed, chain_offset, n_points, n_steps, period, max_rounds,
+                                          C.c_void_p(d_points), C.c_void_p(d_centre_acc), ld, C.c_void_p(stream),
+                                          C.byref(st), C.byref(rs)))
+        return st.as_dict(), rs.as_dict()
+
     def autotune(self) -> int:
         """Pick the fastest chain-kernel configuration for this model; returns threads per chain."""
         t = C.c_int32()
@@ -378,6 +414,15 @@ def sample_batch(samplers, n_points, n_steps: int, d_outs, ld_outs, stream: int 
     st = BatchStats()
     _check(lib().achr_sample_batch(ctxs, k, pts, n_steps, seed, outs, lds, C.c_void_p(stream), C.byref(st), ms))
     return st.as_dict(), list(ms)
+
+
+def gemm_bf16(M: int, N: int, K: int, A0: int, B0: int, C_out: int, lda: int, ldb: int, ldc: int,
+              A1: int = 0, B1: int = 0, stream: int = 0) -> None:
+    """Tensor-core GEMM on device pointers (achr_gemm_bf16): C = A0 B0^T, or with A1/B1
+    given the three hi/lo split products A0 B0^T + A0 B1^T + A1 B0^T."""
+    nsplit = 3 if (A1 and B1) else 1
+    _check(lib().achr_gemm_bf16(M, N, K, nsplit, C.c_void_p(A0), C.c_void_p(A1 or None), lda, C.c_void_p(B0),
+                                C.c_void_p(B1 or None), ldb, C.c_void_p(C_out), ldc, C.c_void_p(stream)))
 
 
 def exported_symbols() -> list[str]:

@@ -15,9 +15,10 @@
 #include <vector>
 
 #include "../../include/achr.h"
-#include "achr_internal.h"
+#include "achr_ctx.h"
 
 using achr::ChainArgs;
+using achr::DevBuf;
 
 namespace {
 
@@ -37,36 +38,6 @@ achr_status cuda_fail(cudaError_t e, const char *what) {
         cudaError_t e_ = (expr);                                \
         if (e_ != cudaSuccess) return cuda_fail(e_, #expr);     \
     } while (0)
-
-// Device buffer that frees itself.
-template <class T>
-struct DevBuf {
-    T *p = nullptr;
-    size_t count = 0;
-    DevBuf() = default;
-    DevBuf(const DevBuf &) = delete;
-    DevBuf &operator=(const DevBuf &) = delete;
-    ~DevBuf() { reset(); }
-    void reset() {
-        if (p) cudaFree(p);
-        p = nullptr;
-        count = 0;
-    }
-    cudaError_t alloc(size_t n) {
-        reset();
-        if (n == 0) n = 1;
-        cudaError_t e = cudaMalloc(&p, n * sizeof(T));
-        if (e == cudaSuccess) count = n;
-        else p = nullptr;
-        return e;
-    }
-    cudaError_t upload(const T *h, size_t n) {
-        cudaError_t e = alloc(n);
-        if (e != cudaSuccess) return e;
-        if (n) e = cudaMemcpy(p, h, n * sizeof(T), cudaMemcpyHostToDevice);
-        return e;
-    }
-};
 
 // FP32 image of a bound for the chain kernel's brackets: round to nearest, an
 // infinite bound becomes a finite stand-in (keeps the bracket arithmetic free
@@ -118,22 +89,6 @@ __global__ void centre_kernel(int n, int W, int ldw, const double *__restrict__ 
 
 }  // namespace
 
-struct achr_ctx {
-    int n = 0, m = 0, W = 0, d = 0, ldw = 0, np = 0;
-    float bound_err = 0.0f;
-    double tuned_rate = 0.0;  // chain-steps per ms on the whole GPU with the tuned configuration (0: not measured)
-    int device = 0;
-    achr_options opt{};
-    std::vector<double> h_lb, h_ub;
-    std::vector<int> h_rowptr, h_colidx;
-    std::vector<double> h_val;
-    DevBuf<double> warmup, c0, A0, val, N, points;
-    DevBuf<double2> lbub;
-    DevBuf<float2> bnd;
-    DevBuf<int> rowptr, colidx;
-    DevBuf<unsigned long long> counters;
-};
-
 extern "C" {
 
 void achr_default_options(achr_options *opt) {
@@ -167,7 +122,7 @@ achr_status validate_options(const achr_options &o) {
     if (o.mode != ACHR_MODE_REFERENCE && o.mode != ACHR_MODE_FEASIBLE) return fail(ACHR_ERR_INVALID, "unknown mode");
     if (o.null_space != ACHR_NULL_SVD_STS && o.null_space != ACHR_NULL_SVD_S)
         return fail(ACHR_ERR_INVALID, "unknown null_space method");
-    if (o.check_period <= 0) return fail(ACHR_ERR_INVALID, "check_period must be positive");
+    if (o.check_period < 0) return fail(ACHR_ERR_INVALID, "check_period must be >= 0 (0: no in-loop checks)");
     if (o.max_attempts <= 0) return fail(ACHR_ERR_INVALID, "max_attempts must be positive");
     if (o.centre_offset != 0 && o.centre_offset != 1) return fail(ACHR_ERR_INVALID, "centre_offset must be 0 or 1");
     if (o.threads_per_chain != 0 && o.threads_per_chain != 32 && o.threads_per_chain != 64 &&
@@ -603,7 +558,7 @@ ChainArgs chain_args(const achr_ctx *ctx, uint64_t seed, uint64_t chain_offset, 
     a.ld_out = ld_out;
     a.seed = seed;
     a.chain_offset = chain_offset;
-    a.check_period = ctx->opt.check_period;
+    a.check_period = ctx->opt.check_period > 0 ? ctx->opt.check_period : 0x7fffffff;
     a.max_attempts = ctx->opt.max_attempts;
     a.centre_offset = ctx->opt.centre_offset;
     a.exact_ratio = ctx->opt.exact_ratio;
@@ -680,7 +635,11 @@ achr_status achr_sample(achr_ctx *ctx, uint64_t seed, uint64_t chain_offset, int
     return ACHR_OK;
 }
 
-void achr_destroy(achr_ctx *ctx) { delete ctx; }
+void achr_destroy(achr_ctx *ctx) {
+    if (!ctx) return;
+    achr::reproj_free(ctx->reproj);
+    delete ctx;
+}
 
 }  // extern "C"
 

@@ -322,7 +322,9 @@ __global__ void __launch_bounds__(BD, (BD <= 256 ? 2 : 1)) achr_chain_kernel(con
         long long buf_col = -1;
         bool inflight = false, any_accepted = a.x_in != nullptr, stuck = false;
         const int s_end = a.step0 + a.T;
-        int chk = a.step0 % a.check_period;  // the reference checks when the step count is a multiple (ACHRCuda.cu:325)
+        // The reference checks when the step count is a multiple of the period
+        // (ACHRCuda.cu:325); a period of INT_MAX stands for "never".
+        int chk = a.check_period == 0x7fffffff ? 1 : a.step0 % a.check_period;
         int tbase = a.step0 - kTbl;
 
         for (int s = a.step0; s < s_end && !stuck && !failed; ++s) {

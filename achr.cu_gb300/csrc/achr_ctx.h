@@ -1,0 +1,62 @@
+// Sampler context shared by the C-ABI translation units.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <vector>
+
+#include "../../include/achr.h"
+#include "achr_internal.h"
+
+namespace achr {
+
+// Device buffer that frees itself.
+template <class T>
+struct DevBuf {
+    T *p = nullptr;
+    size_t count = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf &) = delete;
+    DevBuf &operator=(const DevBuf &) = delete;
+    ~DevBuf() { reset(); }
+    void reset() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        count = 0;
+    }
+    cudaError_t alloc(size_t n) {
+        reset();
+        if (n == 0) n = 1;
+        cudaError_t e = cudaMalloc(&p, n * sizeof(T));
+        if (e == cudaSuccess) count = n;
+        else p = nullptr;
+        return e;
+    }
+    cudaError_t upload(const T *h, size_t n) {
+        cudaError_t e = alloc(n);
+        if (e != cudaSuccess) return e;
+        if (n) e = cudaMemcpy(p, h, n * sizeof(T), cudaMemcpyHostToDevice);
+        return e;
+    }
+};
+
+struct ReprojState;
+void reproj_free(ReprojState *r);  // achr_reproject.cu
+
+}  // namespace achr
+
+struct achr_ctx {
+    int n = 0, m = 0, W = 0, d = 0, ldw = 0, np = 0;
+    float bound_err = 0.0f;
+    double tuned_rate = 0.0;  // chain-steps per ms on the whole GPU with the tuned configuration (0: not measured)
+    int device = 0;
+    achr_options opt{};
+    std::vector<double> h_lb, h_ub;
+    std::vector<int> h_rowptr, h_colidx;  // CSR of S in the model's row order (duplicates summed)
+    std::vector<double> h_val;
+    achr::DevBuf<double> warmup, c0, A0, val, N, points;
+    achr::DevBuf<double2> lbub;
+    achr::DevBuf<float2> bnd;
+    achr::DevBuf<int> rowptr, colidx;  // device CSR: rows sorted longest first
+    achr::DevBuf<unsigned long long> counters;
+    achr::ReprojState *reproj = nullptr;  // batched reprojection operator, built on first use
+};

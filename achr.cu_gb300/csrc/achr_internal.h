@@ -22,6 +22,7 @@ enum CounterSlot {
 
 enum DeviceError : unsigned long long {
     ERR_TMA_TIMEOUT = 1ull,
+    ERR_TC_TIMEOUT = 2ull,  // a tensor-core GEMM pipeline wait expired
 };
 
 // Everything one chain-sampling launch reads (device pointers) and its scalars.
@@ -73,5 +74,23 @@ int chain_alloc_length(int n);
 // Threads-per-chain values worth timing for n (padded length within max_np).
 int chain_candidates(int n, int max_np, int *bds, int cap);
 size_t chain_smem_bytes(int n, int d, int ldw, int block);
+
+// Tensor-core GEMM (achr_tc_gemm.cu): C (M x N, FP32, row-major, ldc) =
+// A0 B0^T (nsplit 1) or A0 B0^T + A0 B1^T + A1 B0^T (nsplit 3); operands BF16
+// row-major with K contiguous, K a multiple of 64, lda/ldb multiples of 8.
+struct TcGemm {
+    int M, N, K, nsplit;
+    const void *A0, *A1;
+    long long lda;
+    const void *B0, *B1;
+    long long ldb;
+    float *C;
+    long long ldc;
+    const unsigned long long *gate = nullptr;  // device word: the launch does nothing when *gate <= gate_max
+    unsigned long long gate_max = 0;
+};
+const char *tc_gemm_check(const TcGemm &g);  // nullptr when the shapes are supported
+cudaError_t launch_tc_gemm(const TcGemm &g, unsigned long long *err, cudaStream_t stream);
+double tc_gemm_flops(const TcGemm &g);
 
 }  // namespace achr

@@ -156,7 +156,7 @@ extern "C" achr_status achr_sample_noalloc(const achr_device_model *m, const ach
     if (n_points < 0 || n_steps < 0 || (n_points > 0 && (!d_points_out || ld_out < n_points)))
         return fail(ACHR_ERR_INVALID, "bad output arguments");
     if (opt.mode != ACHR_MODE_REFERENCE && opt.mode != ACHR_MODE_FEASIBLE) return fail(ACHR_ERR_INVALID, "unknown mode");
-    if (opt.check_period <= 0 || opt.max_attempts <= 0 || (opt.centre_offset != 0 && opt.centre_offset != 1))
+    if (opt.check_period < 0 || opt.max_attempts <= 0 || (opt.centre_offset != 0 && opt.centre_offset != 1))
         return fail(ACHR_ERR_INVALID, "bad options");
     const int np = achr::chain_padded_length(n, opt.threads_per_chain);
     if (np == 0 || np > kMaxRxns) return fail(ACHR_ERR_UNSUPPORTED, "no chain-kernel configuration for this size");
@@ -213,7 +213,7 @@ extern "C" achr_status achr_sample_noalloc(const achr_device_model *m, const ach
     a.ld_out = ld_out;
     a.seed = seed;
     a.chain_offset = chain_offset;
-    a.check_period = opt.check_period;
+    a.check_period = opt.check_period > 0 ? opt.check_period : 0x7fffffff;
     a.max_attempts = opt.max_attempts;
     a.centre_offset = opt.centre_offset;
     a.exact_ratio = opt.exact_ratio;

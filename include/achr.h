@@ -67,7 +67,8 @@ enum {
 typedef struct {
     int32_t mode;             /* ACHR_MODE_* (default REFERENCE) */
     int32_t null_space;       /* ACHR_NULL_* (default SVD_STS) */
-    int32_t check_period;     /* residual check every k-th step (default 10, ACHRCuda.cu:325) */
+    int32_t check_period;     /* residual check every k-th step (default 10, ACHRCuda.cu:325); 0 = never
+                                 (for runs that reproject in batches, achr_sample_periodic) */
     int32_t max_attempts;     /* rejected redraws of one step before a chain stops (default 100000) */
     int32_t centre_offset;    /* 0: centre weights of ACHRCuda.cu:347-348; 1: ACHRSamplerMOD.m:174 */
     int32_t exact_ratio;      /* 1: evaluate every ratio-test candidate in FP64 (diagnostic, slower) */
@@ -154,6 +155,55 @@ achr_status achr_sample_resume(achr_ctx *ctx, uint64_t seed, uint64_t chain_offs
 
 /* Release every device and host resource of the context. */
 void achr_destroy(achr_ctx *ctx);
+
+/* ---- Batched reprojection on the tensor cores and periodic-reprojection
+ * sampling.  The reference reprojects one chain at a time when its residual
+ * check fires (reprojectPoint(2), ACHRCuda.cu:208-230, :338-343); these
+ * reproject every chain of a block at once. ---- */
+
+typedef struct achr_reproj_stats {
+    double residual_before;  /* max |S x|_inf over the chains before the first round */
+    double residual_after;   /* after the last round (measured only when stats are requested) */
+    double gemm_ms;          /* tensor-core GEMM time, summed over chunks and rounds */
+    double total_ms;         /* the whole reprojection on the stream */
+    double gemm_flops;       /* FLOPs of the three BF16 split products */
+    int32_t rounds;          /* passes in which some block of chains was corrected */
+    int32_t rank;            /* rank of S kept by the pseudo-inverse */
+    double lambda_min;       /* smallest kept and largest eigenvalue of S S^T */
+    double lambda_max;
+} achr_reproj_stats;
+
+/* x <- clip(x - S^T (S S^T)^+ S x, lb, ub) for chains 0..P-1 of an n x P
+ * row-major device block (leading dimension ld); the centre accumulators (if
+ * d_centre_acc is non-NULL, same layout) move with the points.  Up to
+ * max_rounds (1..16) passes; a block of chains whose max |S x| is already
+ * within opt.residual_tol is left as it is.  Equals the reference's N (N^T x) followed by its clip; the
+ * residual S x and the update are FP64, the dense (S S^T)^+ product runs on
+ * the tensor cores as three BF16 split products with FP32 accumulation.  The
+ * operator is built on the first call (FP64 eigen-decomposition of S S^T).
+ * Synchronises `stream`. */
+achr_status achr_reproject_batch(achr_ctx *ctx, int32_t n_points, double *d_points, double *d_centre_acc,
+                                 int64_t ld, int32_t max_rounds, void *stream, achr_reproj_stats *stats);
+
+/* T steps of P chains in segments of `period` steps with achr_sample_resume,
+ * each segment followed by achr_reproject_batch over all chains (max_rounds).
+ * d_points and d_centre_acc as for achr_sample_resume; they hold the final
+ * points (feasible to the reprojection's accuracy) and accumulators.  With
+ * opt.check_period = 0 the chain kernel performs no per-chain checks. */
+achr_status achr_sample_periodic(achr_ctx *ctx, uint64_t seed, uint64_t chain_offset, int32_t n_points,
+                                 int32_t n_steps, int32_t period, int32_t max_rounds, double *d_points,
+                                 double *d_centre_acc, int64_t ld, void *stream, achr_stats *stats,
+                                 achr_reproj_stats *rstats);
+
+/* The tensor-core GEMM on its own: C (M x N, FP32, row-major, ldc) = A0 B0^T
+ * (nsplit 1) or A0 B0^T + A0 B1^T + A1 B0^T (nsplit 3, hi/lo split products).
+ * A_s are M x K and B_s are N x K BF16 device matrices, row-major with K
+ * contiguous (leading dimensions lda, ldb in elements, multiples of 8; base
+ * addresses 16-byte aligned); K is a multiple of 64.  No reference
+ * counterpart.  Synchronises `stream`. */
+achr_status achr_gemm_bf16(int32_t M, int32_t N, int32_t K, int32_t nsplit, const void *A0, const void *A1,
+                           int64_t lda, const void *B0, const void *B1, int64_t ldb, float *C, int64_t ldc,
+                           void *stream);
 
 /* ---- Tuning and batched sampling (no counterpart in the reference, which
  * hard-codes 8-thread blocks, ACHRCuda.cu:715, and runs one model per process) ---- */

@@ -120,7 +120,7 @@ typedef struct {
 } oracle_problem;
 
 typedef struct {
-    int32_t check_period;   /* 10 (ACHRCuda.cu:325) */
+    int32_t check_period;   /* 10 (ACHRCuda.cu:325); 0 = never */
     int32_t max_attempts;   /* redraws of one step before the chain is declared stuck */
     int32_t centre_offset;  /* 0: CUDA weights (ACHRCuda.cu:347-348); 1: MATLAB (ACHRSamplerMOD.m:174) */
     int32_t threads;        /* OpenMP threads over chains (<=0: library default) */
@@ -189,7 +189,7 @@ static void run_chain(const oracle_problem *pb, const oracle_options *op, uint64
             /* advNextStep, ACHRCuda.cu:242-249 */
             for (int i = 0; i < n; ++i) x[i] = prev[i] + stepDist * u[i];
             /* ACHRCuda.cu:325-344: residual check every check_period steps */
-            if (s % op->check_period == 0) {
+            if (op->check_period > 0 && s % op->check_period == 0) {
                 st->checks++;
                 double mx = 0.0;
                 for (int row = 0; row < pb->m; ++row) {
@@ -241,7 +241,7 @@ static void run_chain(const oracle_problem *pb, const oracle_options *op, uint64
 int oracle_sample(const oracle_problem *pb, const oracle_options *op, uint64_t seed,
                   uint64_t chain_offset, int32_t P, int32_t T, double *out, oracle_stats *stats_out)
 {
-    if (!pb || !op || !out || pb->n <= 0 || pb->n_warmup <= 0 || P < 0 || T < 0 || op->check_period <= 0)
+    if (!pb || !op || !out || pb->n <= 0 || pb->n_warmup <= 0 || P < 0 || T < 0 || op->check_period < 0)
         return -2;
     oracle_stats total = {0, 0, 0, 0, 0};
     int failed = 0;
