@@ -135,6 +135,7 @@ _SIGNATURES = {
                                     C.POINTER(C.c_double)]),
     "achr_sample_noalloc": (C.c_int, [C.POINTER(DeviceModel), C.POINTER(Options), C.c_uint64, C.c_uint64, C.c_int32,
                                       C.c_int32, C.c_void_p, C.c_int64, C.c_void_p, C.POINTER(Stats)]),
+    "achr_set_directions": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_int32]),
     "achr_reproject_batch": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_int64, C.c_int32,
                                        C.c_void_p, C.POINTER(ReprojStats)]),
     "achr_sample_periodic": (C.c_int, [C.c_void_p, C.c_uint64, C.c_uint64, C.c_int32, C.c_int32, C.c_int32,
@@ -357,6 +358,17 @@ class Sampler:
                                         C.c_void_p(d_points), C.c_void_p(d_centre_acc), ld, C.c_void_p(stream),
                                         C.byref(st) if st is not None else None))
         return st.as_dict() if st is not None else None
+
+    def set_directions(self, dirs=None, d_dirs: int = 0, ld: int = 0, n_dirs: int = 0) -> None:
+        """Hit-and-run along a pool of directions (achr_set_directions): a host (n, K)
+        array, or a device pointer with leading dimension ld; None / 0 returns to ACHR."""
+        if dirs is not None:
+            D = np.asfortranarray(np.asarray(dirs, dtype=np.float64))
+            if D.shape[0] != self.n:
+                raise ValueError(f"directions must be ({self.n}, K)")
+            _check(lib().achr_set_directions(self._ctx, D.ctypes.data_as(C.c_void_p), self.n, D.shape[1]))
+        else:
+            _check(lib().achr_set_directions(self._ctx, C.c_void_p(d_dirs or None), ld, n_dirs))
 
     def reproject(self, n_points: int, d_points: int, ld: int, d_centre_acc: int = 0, max_rounds: int = 1,
                   stream: int = 0, with_stats: bool = True) -> Optional[dict]:

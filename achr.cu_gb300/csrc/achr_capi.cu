@@ -574,12 +574,40 @@ ChainArgs chain_args(const achr_ctx *ctx, uint64_t seed, uint64_t chain_offset, 
     a.A_in = nullptr;
     a.A_out = nullptr;
     a.ld_state = 0;
+    a.hit_and_run = 0;
+    if (ctx->n_dirs > 0) {
+        a.warmup = ctx->dirs.p;
+        a.W = ctx->n_dirs;
+        a.A0 = ctx->zeros.p;
+        a.hit_and_run = 1;
+    }
     return a;
 }
 
 }  // namespace
 
 extern "C" {
+
+achr_status achr_set_directions(achr_ctx *ctx, const double *dirs, int64_t ld, int32_t n_dirs) {
+    if (!ctx) return fail(ACHR_ERR_INVALID, "ctx is NULL");
+    if (n_dirs < 0 || (n_dirs > 0 && (!dirs || ld < ctx->n))) return fail(ACHR_ERR_INVALID, "bad direction pool");
+    if (n_dirs == 0) {
+        ctx->dirs.reset();
+        ctx->zeros.reset();
+        ctx->n_dirs = 0;
+        return ACHR_OK;
+    }
+    ctx->n_dirs = 0;
+    ACHR_CUDA_TRY(ctx->dirs.alloc((size_t)ctx->ldw * n_dirs));
+    ACHR_CUDA_TRY(cudaMemset(ctx->dirs.p, 0, sizeof(double) * (size_t)ctx->ldw * n_dirs));
+    // host or device source (unified addressing decides the direction)
+    ACHR_CUDA_TRY(cudaMemcpy2D(ctx->dirs.p, sizeof(double) * ctx->ldw, dirs, sizeof(double) * ld,
+                               sizeof(double) * ctx->n, n_dirs, cudaMemcpyDefault));
+    ACHR_CUDA_TRY(ctx->zeros.alloc((size_t)ctx->np));
+    ACHR_CUDA_TRY(cudaMemset(ctx->zeros.p, 0, sizeof(double) * (size_t)ctx->np));
+    ctx->n_dirs = n_dirs;
+    return ACHR_OK;
+}
 
 achr_status achr_sample_resume(achr_ctx *ctx, uint64_t seed, uint64_t chain_offset, int32_t n_points, int32_t step0,
                                int32_t n_steps, int32_t resume, double *d_points, double *d_centre_acc, int64_t ld,

@@ -297,6 +297,7 @@ __global__ void __launch_bounds__(BD, (BD <= 256 ? 2 : 1)) achr_chain_kernel(con
     const float dtol_hi = a.dtol_hi, dtol_lo = a.dtol_lo, berr = a.bound_err;
     const float utol32 = a.utol32, mmt32 = a.mmt32;
     const unsigned long long res_tol_bits = (unsigned long long)__double_as_longlong(a.residual_tol);
+    const bool hr = a.hit_and_run != 0;  // directions are the staged columns themselves (no centre)
     unsigned phase = 0, it = 0;
     bool failed = false;
     double worst_res = 0.0, worst_viol = 0.0;
@@ -384,16 +385,28 @@ __global__ void __launch_bounds__(BD, (BD <= 256 ? 2 : 1)) achr_chain_kernel(con
                     inflight = false;
                 }
 
-                // Phase A: d = w_r - A / (W + t)  (reference ACHRCuda.cu:260-264)
+                // Phase A: d = w_r - A / (W + t)  (reference ACHRCuda.cu:260-264);
+                // in hit-and-run mode the staged column is the direction itself.
                 double dreg[EPT];
                 float ss = 0.0f;
+                if (hr) {
 #pragma unroll
-                for (int k = 0; k < EPT; ++k) {
-                    const int i = tid + k * BD;
-                    const double dk = fma(As[i], ninv, ws[i]);
-                    dreg[k] = dk;
-                    const float d32 = f64_to_f32_rz(dk);
-                    ss = fmaf(d32, d32, ss);
+                    for (int k = 0; k < EPT; ++k) {
+                        const int i = tid + k * BD;
+                        const double dk = ws[i];
+                        dreg[k] = dk;
+                        const float d32 = f64_to_f32_rz(dk);
+                        ss = fmaf(d32, d32, ss);
+                    }
+                } else {
+#pragma unroll
+                    for (int k = 0; k < EPT; ++k) {
+                        const int i = tid + k * BD;
+                        const double dk = fma(As[i], ninv, ws[i]);
+                        dreg[k] = dk;
+                        const float d32 = f64_to_f32_rz(dk);
+                        ss = fmaf(d32, d32, ss);
+                    }
                 }
 #pragma unroll
                 for (int o = 16; o; o >>= 1) ss += __shfl_xor_sync(0xffffffffu, ss, o);
@@ -618,7 +631,20 @@ __global__ void __launch_bounds__(BD, (BD <= 256 ? 2 : 1)) achr_chain_kernel(con
                 // check_period steps (:325-344), clip + centre (:193-206, :347-350).
                 const bool check = chk == 0;
                 chk = (chk + 1 == a.check_period) ? 0 : chk + 1;
-                if (!check) {
+                if (!check && hr) {  // hit-and-run: no centre to update
+                    unsigned edge = 0;
+#pragma unroll
+                    for (int k = 0; k < EPT; ++k) {
+                        const int i = tid + k * BD;
+                        const double xn = fma(sstep, dreg[k], xs[i]);
+                        xs[i] = xn;
+                        if (!surely_inside(f64_to_f32_rz(xn), __ldg(a.bnd + i), berr)) edge |= 1u << k;
+                    }
+                    for (; edge; edge &= edge - 1) {
+                        const int i = tid + (__ffs(edge) - 1) * BD;
+                        xs[i] = clip_exact(xs[i], ld_lbub(a.lbub + i));
+                    }
+                } else if (!check) {
                     unsigned edge = 0;  // bit k: not provably inside the box, clip exactly below
 #pragma unroll
                     for (int k = 0; k < EPT; ++k) {
@@ -698,14 +724,17 @@ __global__ void __launch_bounds__(BD, (BD <= 256 ? 2 : 1)) achr_chain_kernel(con
                     for (int k = 0; k < EPT; ++k) {
                         const int i = tid + k * BD;
                         const double xv = xs[i];
-                        if (surely_inside(f64_to_f32_rz(xv), __ldg(a.bnd + i), berr)) As[i] += xv;
-                        else edge |= 1u << k;
+                        if (surely_inside(f64_to_f32_rz(xv), __ldg(a.bnd + i), berr)) {
+                            if (!hr) As[i] += xv;
+                        } else {
+                            edge |= 1u << k;
+                        }
                     }
                     for (; edge; edge &= edge - 1) {
                         const int i = tid + (__ffs(edge) - 1) * BD;
                         const double xc = clip_exact(xs[i], ld_lbub(a.lbub + i));
                         xs[i] = xc;
-                        As[i] += xc;
+                        if (!hr) As[i] += xc;
                     }
                 }
                 if (tid == 0) ++cnt[CNT_ACCEPTED];

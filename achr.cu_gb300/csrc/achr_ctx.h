@@ -59,4 +59,7 @@ struct achr_ctx {
     achr::DevBuf<int> rowptr, colidx;  // device CSR: rows sorted longest first
     achr::DevBuf<unsigned long long> counters;
     achr::ReprojState *reproj = nullptr;  // batched reprojection operator, built on first use
+    achr::DevBuf<double> dirs;   // hit-and-run direction pool, n x n_dirs (leading dimension ldw)
+    int n_dirs = 0;              // 0: ACHR directions (warmup point minus centre)
+    achr::DevBuf<double> zeros;  // np zeros: the (unused) centre accumulator of hit-and-run chains
 };

@@ -53,6 +53,7 @@ struct ChainArgs {
     unsigned long long seed, chain_offset;
     int check_period, max_attempts, centre_offset, exact_ratio;
     int final_project;          // 1: project+clip emitted points whose residual exceeds feasibility_tol
+    int hit_and_run;            // 1: `warmup` holds directions; d = column r, no centre (A stays as loaded)
     double residual_tol, max_min_tol, u_tol, d_tol, feasibility_tol;
     unsigned long long *counters;  // CNT_SLOTS entries
 };

@@ -35,6 +35,9 @@ class SyntheticSpec:
 # with 100,000 chains x 2000 steps.
 SMALL = SyntheticSpec(n_rxns=95, n_mets=72, irreversible_frac=0.25, n_exchange=20, exchange_bound=10.0, seed=1)
 GENOME = SyntheticSpec(n_rxns=3742, n_mets=2766, irreversible_frac=0.30, n_exchange=150, exchange_bound=20.0, seed=2)
+# The 5063 x 7440 model of the mixed-precision reprojection and learned-
+# preconditioner workloads (262,144 chains x 5000 steps), same law as GENOME.
+LARGE = SyntheticSpec(n_rxns=7440, n_mets=5063, irreversible_frac=0.30, n_exchange=150, exchange_bound=20.0, seed=4)
 
 
 def make_model(spec: SyntheticSpec):

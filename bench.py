@@ -38,6 +38,7 @@ WORKLOADS = {
     # name: (spec attribute, chains, steps)
     "genome": ("GENOME", 100_000, 2000),
     "small": ("SMALL", 1000, 1000),
+    "large": ("LARGE", 262_144, 5000),
 }
 
 
@@ -55,6 +56,8 @@ def parse_args():
     ap.add_argument("--ess", type=int, nargs=4, metavar=("CHAINS", "BURNIN", "SEGMENTS", "STEPS"),
                     help="min-ESS/s and max R-hat from trace snapshots: CHAINS chains, BURNIN steps, then SEGMENTS "
                          "snapshots STEPS steps apart")
+    ap.add_argument("--large-chains", type=int, default=262_144, help="chains of the large workload")
+    ap.add_argument("--large-steps", type=int, default=200, help="timed steps of the large workload")
     ap.add_argument("--profile-case", type=int, nargs=2, metavar=("CHAINS", "STEPS"),
                     help="run two launches of CHAINS x STEPS of the workload and print their times (ncu captures)")
     return ap.parse_args()
@@ -84,7 +87,18 @@ def profile_traffic_per_chain_step(workload):
     return float(m.group(1)) if m else None
 
 
-def build_inputs(workload, pkg, synth):
+def gpu_null_space_fn(pkg):
+    """Null-space basis of a dense matrix through the library (cuSOLVER), for warmup generation."""
+    def null_space(SF):
+        r, c = np.nonzero(SF)
+        m = pkg.HostModel(SF.shape[1], SF.shape[0], r, c, SF[r, c], np.full(SF.shape[1], -1.0),
+                          np.full(SF.shape[1], 1.0))
+        with pkg.Sampler(m, np.zeros((SF.shape[1], 1))) as tmp:
+            return tmp.null_space()
+    return null_space
+
+
+def build_inputs(workload, pkg, synth, null_space=None):
     """Model arrays, dense S and warmup points (numpy; identical for both arms).
     Cached under /tmp so the two arms of one run share the set-up work."""
     spec_name, P, T = WORKLOADS[workload]
@@ -96,7 +110,7 @@ def build_inputs(workload, pkg, synth):
     if cache.exists():
         warm = np.load(cache)["warm"]
     else:
-        warm = synth.interior_chord_warmup(S, lb, ub, W, seed=spec.seed + 17)
+        warm = synth.interior_chord_warmup(S, lb, ub, W, seed=spec.seed + 17, null_space=null_space)
         np.savez(cache, warm=warm)
     model = pkg.HostModel(spec.n_rxns, spec.n_mets, row, col, val, lb, ub)
     return spec, model, S, warm, P, T
@@ -525,8 +539,128 @@ def run_ess(args):
     return 0
 
 
+def load_tensor_peak():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        if "bf16_tflops" in d:
+            return float(d["bf16_tflops"]), "measured bf16_tflops (cuBLAS, burst)"
+    return 1900.0, "fallback"
+
+
+def fp64_reprojection(S, lb, ub, X):
+    """FP64 oracle of one reprojection pass: clip(x - S^T (S S^T)^+ S x), numpy."""
+    lam, U = np.linalg.eigh(S @ S.T)
+    keep = lam > S.shape[0] * lam.max() * 2.2204e-16
+    R = S @ X
+    Z = U[:, keep] @ ((U[:, keep].T @ R) / lam[keep][:, None])
+    return np.clip(X - S.T @ Z, lb[:, None], ub[:, None])
+
+
+def run_large(args):
+    """Mixed-precision reprojection workload: 5063 x 7440 model, chains reprojected
+    every 100 steps by the batched tensor-core reprojection (achr_sample_periodic,
+    no per-chain checks), against plain ACHR with the reference's per-chain FP64
+    checks on the same chains.  The timed run is a bounded slice of the 5000-step
+    workload (--large-steps, default 200 = two reprojections); chain-steps/s does
+    not depend on the slice length.  Prints one JSON line."""
+    import torch
+
+    import __graft_entry__ as ge
+
+    pkg = ge.load_package()
+    pkg.lib()
+    import importlib
+    synth = importlib.import_module("achr_gb300.synthetic")
+    t_setup = time.perf_counter()
+    spec, model, S, warm, P, T = build_inputs("large", pkg, synth, null_space=gpu_null_space_fn(pkg))
+    P = args.large_chains
+    period, Tr = 100, args.large_steps
+    n = spec.n_rxns
+    smp = pkg.Sampler(model, warm, check_period=0)
+    tpc = smp.autotune()
+    x = torch.zeros((n, P), dtype=torch.float64, device="cuda")
+    a = torch.zeros_like(x)
+    stream = torch.cuda.current_stream().cuda_stream
+    t_op = time.perf_counter()
+    smp.reproject(1, x.data_ptr(), P)  # builds (S S^T)^+ and its BF16 split
+    operator_s = time.perf_counter() - t_op
+    setup_s = time.perf_counter() - t_setup
+    smp.sample_periodic(P, period, period, x.data_ptr(), a.data_ptr(), P, stream=stream, seed=args.seed)  # warm-up
+    clocks = ClockSampler(0)
+    clocks.start()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    ev0.record()
+    st, rs = smp.sample_periodic(P, Tr, period, x.data_ptr(), a.data_ptr(), P, stream=stream, seed=args.seed + 1)
+    ev1.record()
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = ev0.elapsed_time(ev1)
+    # Reprojection accuracy against the FP64 oracle on 64 chains: one more
+    # segment without reprojection, snapshot, then one reprojection pass.
+    smp.sample_resume(P, Tr, period, True, x.data_ptr(), a.data_ptr(), P, stream=stream, seed=args.seed + 1)
+    Xs = x[:, :64].cpu().numpy()
+    r1 = smp.reproject(P, x.data_ptr(), P, d_centre_acc=a.data_ptr(), max_rounds=1, stream=stream)
+    got = x[:, :64].cpu().numpy()
+    ref = fp64_reprojection(S, model.lb, model.ub, Xs)
+    moved = float(np.abs(ref - Xs).max())
+    err = float(np.abs(got - ref).max())
+    smp.close()
+    del x, a
+    torch.cuda.empty_cache()
+    # Plain ACHR on the same chains: per-chain residual check every 10 steps,
+    # FP64 reprojection of a chain when it fires (reference semantics).
+    plain = pkg.Sampler(model, warm)
+    plain.autotune()
+    out = torch.empty((n, P), dtype=torch.float64, device="cuda")
+    plain.sample_device(P, 20, out.data_ptr(), P, stream=stream, seed=args.seed)
+    torch.cuda.synchronize()
+    ev0.record()
+    pst = plain.sample_device(P, Tr, out.data_ptr(), P, stream=stream, seed=args.seed + 1, with_stats=True)
+    ev1.record()
+    torch.cuda.synchronize()
+    plain_ms = ev0.elapsed_time(ev1)
+    plain.close()
+    tpeak, tpeak_kind = load_tensor_peak()
+    gemm_tflops = rs["gemm_flops"] / (rs["gemm_ms"] * 1e-3) / 1e12 if rs["gemm_ms"] > 0 else None
+    peak, peak_kind = load_peaks()
+    alg = synth.ideal_bytes_per_chain_step(n) * P * Tr
+    line = {
+        "metric": METRIC, "value": st["accepted"] / (ms * 1e-3), "unit": METRIC, "n_gpus": 1, "steps": 1,
+        "warmup": 1, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64 (reprojection GEMM: 3 x bf16 split, fp32 accumulate)", "data": "synthetic",
+        "config": {"workload": f"large: {spec.n_mets}x{n} synthetic model, W={warm.shape[1]}, {P} chains x {Tr} "
+                               f"steps (of {T}), batched tensor-core reprojection every {period} steps, "
+                               f"no per-chain checks", "threads_per_chain": tpc},
+        "roofline": {"bound": "hbm", "achieved": alg / (ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
+                     "frac": alg / (ms * 1e-3) / 1e9 / peak, "peak_source": f"{peak_kind} hbm_gbs"},
+        "reprojection": {
+            "passes": rs["rounds"], "gemm_ms": rs["gemm_ms"], "total_ms": rs["total_ms"],
+            "share_of_run": rs["total_ms"] / ms, "gemm_tflops": gemm_tflops, "tensor_peak_tflops": tpeak,
+            "tensor_frac": (gemm_tflops / tpeak) if gemm_tflops else None, "tensor_peak_source": tpeak_kind,
+            "residual_before": rs["residual_before"], "residual_after": rs["residual_after"],
+            "rank": rs["rank"], "kappa": rs["lambda_max"] / rs["lambda_min"] if rs["lambda_min"] > 0 else None,
+            "oracle_check": {"chains": 64, "max_abs_err": err, "max_correction": moved,
+                             "rel_err": err / moved if moved > 0 else None,
+                             "residual_before": r1["residual_before"], "residual_after": r1["residual_after"],
+                             "max_abs_Sv": float(np.abs(S @ got).max())},
+            "operator_setup_s": operator_s,
+        },
+        "plain_reference_semantics": {"value": pst["accepted"] / (plain_ms * 1e-3), "ms": plain_ms,
+                                      "checks": pst["checks"], "reprojections": pst["reprojections"],
+                                      "max_residual": pst["max_residual"]},
+        "sampler": {k: st[k] for k in ("accepted", "rejected", "stuck_chains", "max_residual", "max_bound_violation")},
+        "clocks": clk, "setup_s": setup_s,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     args = parse_args()
+    if args.workload == "large" and args.impl == "gb300" and not args.ess:
+        return run_large(args)
     if args.ess:
         return run_ess(args)
     if args.workload == "batch64":

@@ -156,6 +156,67 @@ achr_status achr_sample_resume(achr_ctx *ctx, uint64_t seed, uint64_t chain_offs
 /* Release every device and host resource of the context. */
 void achr_destroy(achr_ctx *ctx);
 
+/* ---- Hit-and-run along a pool of directions (no reference counterpart) ----
+ * Replaces ACHR's direction (a random warmup point minus the running centre,
+ * ACHRCuda.cu:260-264) by a random column of a fixed pool: each step draws a
+ * pool index from the same Philox stream as the warmup index, moves along
+ * that column with the reference's ratio test and step draw, clips, and keeps
+ * no centre.  The direction distribution is symmetric and independent of the
+ * state, so the chain keeps the uniform target.  dirs is n x n_dirs
+ * column-major (leading dimension ld >= n), host or device memory; every
+ * column should lie in the null space of S.  n_dirs = 0 returns the context
+ * to ACHR.  Chains start at the warmup centre in either mode. */
+achr_status achr_set_directions(achr_ctx *ctx, const double *dirs, int64_t ld, int32_t n_dirs);
+
+/* ---- Learned direction preconditioner (no reference counterpart) ----
+ * A low-rank-plus-diagonal linear map L = [diag(exp(s)), U] (d x (d + r)) in
+ * null-space coordinates, fitted to samples y = N^T (x - mu) of the plain
+ * sampler by the Gaussian KL loss 1/2 tr(C^-1 Sigma) + 1/2 log det C with
+ * C = L L^T = diag(exp(2 s)) + U U^T (minibatch Sigma, Adam), all on the GPU.
+ * Its directions N L z, z ~ N(0, I), drive hit-and-run (achr_set_directions)
+ * through a pool of K of them.  s is d floats, U is d x r row-major, Y is
+ * d x n_samples row-major (leading dimension ldy), all device memory. */
+typedef struct achr_precond_options {
+    int32_t iterations;    /* Adam steps (2000) */
+    int32_t batch;         /* samples per step (4096) */
+    float learning_rate;   /* 0.01 */
+    float beta1, beta2;    /* 0.9, 0.999 */
+    float eps;             /* 1e-8 */
+    uint64_t seed;         /* order in which minibatches are visited */
+} achr_precond_options;
+
+typedef struct achr_precond_stats {
+    double loss_first;     /* mean loss over the first 20 minibatches */
+    double loss_last;      /* mean loss over the last 20 minibatches */
+    double train_ms;
+    int32_t iterations;
+} achr_precond_stats;
+
+void achr_precond_default_options(achr_precond_options *opt);
+
+/* Y (d x P, row-major, leading dimension ldy, FP32) = N^T (x - mu) for the
+ * chains of an n x P row-major block of points (mu: n doubles or NULL), as a
+ * tensor-core GEMM with three BF16 split products.  Synchronises `stream`. */
+achr_status achr_null_coords(achr_ctx *ctx, int32_t n_points, const double *d_points, int64_t ld, const double *d_mu,
+                             float *d_Y, int64_t ldy, void *stream);
+
+/* Loss and gradients (ds: d floats, dU: d x r) for one minibatch Y (d x B). */
+achr_status achr_precond_loss_grad(int32_t d, int32_t r, int32_t B, const float *d_s, const float *d_U,
+                                   const float *d_Y, int64_t ldy, float *loss_out, float *d_gs, float *d_gU,
+                                   void *stream);
+
+/* opt.iterations Adam steps from the given s, U (updated in place) over
+ * minibatches of consecutive columns of Y.  Synchronises `stream`. */
+achr_status achr_precond_train(int32_t d, int32_t r, int32_t n_samples, const float *d_Y, int64_t ldy,
+                               const achr_precond_options *opt, float *d_s, float *d_U, void *stream,
+                               achr_precond_stats *stats);
+
+/* Pool of n_dirs directions N (exp(s) z1 + U z2), z ~ N(0, I) from Philox
+ * keyed by seed, computed in FP64 (the directions lie in the null space of S
+ * to rounding), installed with achr_set_directions. */
+achr_status achr_precond_pool(achr_ctx *ctx, int32_t r, const float *d_s, const float *d_U, int32_t n_dirs,
+                              uint64_t seed);
+
 /* ---- Batched reprojection on the tensor cores and periodic-reprojection
  * sampling.  The reference reprojects one chain at a time when its residual
  * check fires (reprojectPoint(2), ACHRCuda.cu:208-230, :338-343); these

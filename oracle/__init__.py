@@ -59,7 +59,7 @@ class _Problem(C.Structure):
 class _Options(C.Structure):
     _fields_ = [
         ("check_period", C.c_int32), ("max_attempts", C.c_int32), ("centre_offset", C.c_int32),
-        ("threads", C.c_int32),
+        ("threads", C.c_int32), ("hit_and_run", C.c_int32), ("reserved", C.c_int32),
         ("residual_tol", C.c_double), ("max_min_tol", C.c_double), ("u_tol", C.c_double), ("d_tol", C.c_double),
     ]
 
@@ -153,9 +153,11 @@ class Problem:
                            ip(self.ci), dp(self.vv), self.N.shape[1], dp(self.N), dp(self.c0))
 
     def sample(self, seed, n_points, n_steps, chain_offset=0, check_period=10, max_attempts=100000, centre_offset=0,
-               threads=0, residual_tol=1e-9, max_min_tol=1e-9, u_tol=1e-9, d_tol=1e-14):
-        """Returns ((n, P) points, stats dict)."""
-        op = _Options(check_period, max_attempts, centre_offset, threads, residual_tol, max_min_tol, u_tol, d_tol)
+               threads=0, residual_tol=1e-9, max_min_tol=1e-9, u_tol=1e-9, d_tol=1e-14, hit_and_run=False):
+        """Returns ((n, P) points, stats dict).  hit_and_run: the warmup matrix holds
+        directions (u = w_r / |w_r|, no centre) and chains start at centre_point."""
+        op = _Options(check_period, max_attempts, centre_offset, threads, int(hit_and_run), 0, residual_tol,
+                      max_min_tol, u_tol, d_tol)
         out = np.zeros((self.n, n_points))
         st = _Stats()
         rc = lib().oracle_sample(C.byref(self.pb), C.byref(op), seed, chain_offset, n_points, n_steps,

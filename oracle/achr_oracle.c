@@ -34,6 +34,9 @@
  *     thrust's end() iterator, ACHRCuda.cu:283-288) counts as a rejection;
  *   - a step that is rejected max_attempts times in a row stops the chain and
  *     is reported (the reference loops forever).
+ * Extension without a reference counterpart: hit_and_run = 1 runs the same
+ * loop with the warmup matrix read as a pool of directions (u = w_r/|w_r|,
+ * no centre), the form the learned direction pool is sampled with.
  *
  * Build: oracle/build_oracle.sh (gcc -O2 -fopenmp -ffp-contract=off).
  */
@@ -124,6 +127,8 @@ typedef struct {
     int32_t max_attempts;   /* redraws of one step before the chain is declared stuck */
     int32_t centre_offset;  /* 0: CUDA weights (ACHRCuda.cu:347-348); 1: MATLAB (ACHRSamplerMOD.m:174) */
     int32_t threads;        /* OpenMP threads over chains (<=0: library default) */
+    int32_t hit_and_run;    /* 1: `warmup` holds directions, u = w_r / |w_r|, no centre (c = 0, never updated) */
+    int32_t reserved;
     double residual_tol;    /* 1e-9 (ACHRCuda.cu:338) */
     double max_min_tol;     /* 1e-9 (ACHRCuda.cu:505) */
     double u_tol;           /* 1e-9 (ACHRCuda.cu:508) */
@@ -149,7 +154,7 @@ static void run_chain(const oracle_problem *pb, const oracle_options *op, uint64
     const double uTol = op->u_tol, dTol = op->d_tol, maxMinTol = op->max_min_tol;
     /* ACHRCuda.cu:376-379: per-chain centre and prevPoint start at the global centre;
      * ACHRCuda.cu:739: the output points start at zero. */
-    for (int i = 0; i < n; ++i) { c[i] = pb->centre[i]; prev[i] = pb->centre[i]; x[i] = 0.0; }
+    for (int i = 0; i < n; ++i) { c[i] = op->hit_and_run ? 0.0 : pb->centre[i]; prev[i] = pb->centre[i]; x[i] = 0.0; }
     int stuck = 0;
     for (int32_t s = 0; s < T && !stuck; ++s) {
         const double Ustep = oracle_step_uniform(seed, chain, (uint32_t)s);
@@ -224,7 +229,7 @@ static void run_chain(const oracle_problem *pb, const oracle_options *op, uint64
                 if (x[i] > pb->ub[i]) x[i] = pb->ub[i];
                 else if (x[i] < pb->lb[i]) x[i] = pb->lb[i];
                 prev[i] = x[i];
-                c[i] = alpha * c[i] + beta * x[i];
+                if (!op->hit_and_run) c[i] = alpha * c[i] + beta * x[i];
             }
             st->accepted++;
             break;
