@@ -113,6 +113,21 @@ class ReprojStats(C.Structure):
         return {name: getattr(self, name) for name, _ in self._fields_}
 
 
+class PrecondOptions(C.Structure):
+    _fields_ = [
+        ("iterations", C.c_int32), ("batch", C.c_int32), ("learning_rate", C.c_float), ("beta1", C.c_float),
+        ("beta2", C.c_float), ("eps", C.c_float), ("seed", C.c_uint64),
+    ]
+
+
+class PrecondStats(C.Structure):
+    _fields_ = [("loss_first", C.c_double), ("loss_last", C.c_double), ("train_ms", C.c_double),
+                ("iterations", C.c_int32)]
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
 # Every symbol include/achr.h declares, with its ctypes signature.
 _SIGNATURES = {
     "achr_default_options": (None, [C.POINTER(Options)]),
@@ -136,6 +151,17 @@ _SIGNATURES = {
     "achr_sample_noalloc": (C.c_int, [C.POINTER(DeviceModel), C.POINTER(Options), C.c_uint64, C.c_uint64, C.c_int32,
                                       C.c_int32, C.c_void_p, C.c_int64, C.c_void_p, C.POINTER(Stats)]),
     "achr_set_directions": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_int32]),
+    "achr_get_n_directions": (C.c_int32, [C.c_void_p]),
+    "achr_get_directions": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "achr_precond_default_options": (None, [C.POINTER(PrecondOptions)]),
+    "achr_null_coords": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_int64,
+                                   C.c_void_p]),
+    "achr_precond_loss_grad": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p,
+                                         C.c_int64, C.POINTER(C.c_float), C.c_void_p, C.c_void_p, C.c_void_p]),
+    "achr_precond_train": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_int64,
+                                     C.POINTER(PrecondOptions), C.c_void_p, C.c_void_p, C.c_void_p,
+                                     C.POINTER(PrecondStats)]),
+    "achr_precond_pool": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_int32, C.c_uint64]),
     "achr_reproject_batch": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_int64, C.c_int32,
                                        C.c_void_p, C.POINTER(ReprojStats)]),
     "achr_sample_periodic": (C.c_int, [C.c_void_p, C.c_uint64, C.c_uint64, C.c_int32, C.c_int32, C.c_int32,
@@ -370,6 +396,24 @@ class Sampler:
         else:
             _check(lib().achr_set_directions(self._ctx, C.c_void_p(d_dirs or None), ld, n_dirs))
 
+    def directions(self) -> np.ndarray:
+        """The installed hit-and-run direction pool, (n, K); empty in ACHR mode."""
+        k = lib().achr_get_n_directions(self._ctx)
+        out = np.zeros((self.n, k), order="F")
+        if k:
+            _check(lib().achr_get_directions(self._ctx, out.ctypes.data_as(C.c_void_p)))
+        return out
+
+    def null_coords(self, n_points: int, d_points: int, ld: int, d_Y: int, ldy: int, d_mu: int = 0,
+                    stream: int = 0) -> None:
+        """Y (d x P FP32, device) = N^T (x - mu) for an n x ld device block of points."""
+        _check(lib().achr_null_coords(self._ctx, n_points, C.c_void_p(d_points), ld, C.c_void_p(d_mu or None),
+                                      C.c_void_p(d_Y), ldy, C.c_void_p(stream)))
+
+    def precond_pool(self, rank: int, d_s: int, d_U: int, n_dirs: int, seed: int = 0) -> None:
+        """Install a pool of n_dirs directions N (exp(s) z1 + U z2) (achr_precond_pool)."""
+        _check(lib().achr_precond_pool(self._ctx, rank, C.c_void_p(d_s), C.c_void_p(d_U or None), n_dirs, seed))
+
     def reproject(self, n_points: int, d_points: int, ld: int, d_centre_acc: int = 0, max_rounds: int = 1,
                   stream: int = 0, with_stats: bool = True) -> Optional[dict]:
         """Reproject chains 0..P-1 of an n x ld device block in place (achr_reproject_batch)."""
@@ -435,6 +479,33 @@ def gemm_bf16(M: int, N: int, K: int, A0: int, B0: int, C_out: int, lda: int, ld
     nsplit = 3 if (A1 and B1) else 1
     _check(lib().achr_gemm_bf16(M, N, K, nsplit, C.c_void_p(A0), C.c_void_p(A1 or None), lda, C.c_void_p(B0),
                                 C.c_void_p(B1 or None), ldb, C.c_void_p(C_out), ldc, C.c_void_p(stream)))
+
+
+def precond_options(**overrides) -> PrecondOptions:
+    o = PrecondOptions()
+    lib().achr_precond_default_options(C.byref(o))
+    for k, v in overrides.items():
+        setattr(o, k, v)
+    return o
+
+
+def precond_loss_grad(d: int, r: int, B: int, d_s: int, d_U: int, d_Y: int, ldy: int, d_gs: int, d_gU: int,
+                      stream: int = 0) -> float:
+    """Loss and gradients of the preconditioner on one minibatch (device pointers)."""
+    loss = C.c_float()
+    _check(lib().achr_precond_loss_grad(d, r, B, C.c_void_p(d_s), C.c_void_p(d_U), C.c_void_p(d_Y), ldy,
+                                        C.byref(loss), C.c_void_p(d_gs), C.c_void_p(d_gU), C.c_void_p(stream)))
+    return loss.value
+
+
+def precond_train(d: int, r: int, n_samples: int, d_Y: int, ldy: int, d_s: int, d_U: int, stream: int = 0,
+                  **options) -> dict:
+    """Fit s, U (device, updated in place) to the samples Y (achr_precond_train)."""
+    opt = precond_options(**options)
+    st = PrecondStats()
+    _check(lib().achr_precond_train(d, r, n_samples, C.c_void_p(d_Y), ldy, C.byref(opt), C.c_void_p(d_s),
+                                    C.c_void_p(d_U), C.c_void_p(stream), C.byref(st)))
+    return st.as_dict()
 
 
 def exported_symbols() -> list[str]:

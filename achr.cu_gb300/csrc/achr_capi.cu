@@ -609,6 +609,16 @@ achr_status achr_set_directions(achr_ctx *ctx, const double *dirs, int64_t ld, i
     return ACHR_OK;
 }
 
+achr_status achr_get_directions(const achr_ctx *ctx, double *dirs_out) {
+    if (!ctx || !dirs_out) return fail(ACHR_ERR_INVALID, "NULL argument");
+    if (ctx->n_dirs == 0) return ACHR_OK;
+    ACHR_CUDA_TRY(cudaMemcpy2D(dirs_out, sizeof(double) * ctx->n, ctx->dirs.p, sizeof(double) * ctx->ldw,
+                               sizeof(double) * ctx->n, ctx->n_dirs, cudaMemcpyDefault));
+    return ACHR_OK;
+}
+
+int32_t achr_get_n_directions(const achr_ctx *ctx) { return ctx ? ctx->n_dirs : 0; }
+
 achr_status achr_sample_resume(achr_ctx *ctx, uint64_t seed, uint64_t chain_offset, int32_t n_points, int32_t step0,
                                int32_t n_steps, int32_t resume, double *d_points, double *d_centre_acc, int64_t ld,
                                void *stream, achr_stats *stats) {

@@ -56,6 +56,17 @@ def parse_args():
     ap.add_argument("--ess", type=int, nargs=4, metavar=("CHAINS", "BURNIN", "SEGMENTS", "STEPS"),
                     help="min-ESS/s and max R-hat from trace snapshots: CHAINS chains, BURNIN steps, then SEGMENTS "
                          "snapshots STEPS steps apart")
+    ap.add_argument("--learned", type=int, nargs=4, metavar=("CHAINS", "BURNIN", "SEGMENTS", "STEPS"),
+                    help="learned-preconditioned hit-and-run against plain ACHR on this ESS schedule")
+    ap.add_argument("--train-chains", type=int, default=65536)
+    ap.add_argument("--train-burnin", type=int, default=2000)
+    ap.add_argument("--train-snapshots", type=int, default=8)
+    ap.add_argument("--train-gap", type=int, default=250)
+    ap.add_argument("--rank", type=int, default=256)
+    ap.add_argument("--iters", type=int, default=2000)
+    ap.add_argument("--batch", type=int, default=4096)
+    ap.add_argument("--lr", type=float, default=0.01)
+    ap.add_argument("--pool", type=int, default=16384)
     ap.add_argument("--large-chains", type=int, default=262_144, help="chains of the large workload")
     ap.add_argument("--large-steps", type=int, default=200, help="timed steps of the large workload")
     ap.add_argument("--profile-case", type=int, nargs=2, metavar=("CHAINS", "STEPS"),
@@ -484,6 +495,29 @@ def run_batch(args):
     return 0
 
 
+def ess_trace(smp, M, B, K, L, seed, stream):
+    """Chains from the warmup centre: B burn-in steps, then K segments of L steps
+    (achr_sample_resume); the points after every segment are the draws.
+    Returns (draws (chains, draws, fluxes), device ms of all launches, chain-steps)."""
+    import torch
+
+    n = smp.n
+    pts = torch.zeros((n, M), dtype=torch.float64, device="cuda")
+    acc = torch.zeros((n, M), dtype=torch.float64, device="cuda")
+    trace = torch.empty((K, n, M), dtype=torch.float64, device="cuda")
+    st = smp.sample_resume(M, 0, B, False, pts.data_ptr(), acc.data_ptr(), M, stream=stream, seed=seed,
+                           with_stats=True)
+    ms, steps = st["kernel_ms"], st["accepted"]
+    for k in range(K):
+        st = smp.sample_resume(M, B + k * L, L, True, pts.data_ptr(), acc.data_ptr(), M, stream=stream, seed=seed,
+                               with_stats=True)
+        ms += st["kernel_ms"]
+        steps += st["accepted"]
+        trace[k].copy_(pts)
+    torch.cuda.synchronize()
+    return trace.permute(2, 0, 1).cpu().numpy(), ms, steps
+
+
 def run_ess(args):
     """min over fluxes of bulk ESS per second of sampling, and max split-R-hat.
 
@@ -500,27 +534,12 @@ def run_ess(args):
     import importlib
     synth = importlib.import_module("achr_gb300.synthetic")
     diag = importlib.import_module("achr_gb300.diagnostics")
-    spec, model, S, warm, _, _ = build_inputs(args.workload, pkg, synth)
+    spec, model, S, warm, _, _ = build_inputs(args.workload, pkg, synth, null_space=gpu_null_space_fn(pkg))
     M, B, K, L = args.ess
     n = spec.n_rxns
     smp = pkg.Sampler(model, warm)
-    pts = torch.zeros((n, M), dtype=torch.float64, device="cuda")
-    acc = torch.zeros((n, M), dtype=torch.float64, device="cuda")
-    trace = torch.empty((K, n, M), dtype=torch.float64, device="cuda")
     stream = torch.cuda.current_stream().cuda_stream
-    ms = 0.0
-    st = smp.sample_resume(M, 0, B, False, pts.data_ptr(), acc.data_ptr(), M, stream=stream, seed=args.seed,
-                           with_stats=True)
-    ms += st["kernel_ms"]
-    acc_steps = st["accepted"]
-    for k in range(K):
-        st = smp.sample_resume(M, B + k * L, L, True, pts.data_ptr(), acc.data_ptr(), M, stream=stream,
-                               seed=args.seed, with_stats=True)
-        ms += st["kernel_ms"]
-        acc_steps += st["accepted"]
-        trace[k].copy_(pts)
-    torch.cuda.synchronize()
-    draws = trace.permute(2, 0, 1).cpu().numpy()  # (chains, draws, fluxes)
+    draws, ms, acc_steps = ess_trace(smp, M, B, K, L, args.seed, stream)
     t0 = time.perf_counter()
     summ = diag.summarize(draws)
     diag_s = time.perf_counter() - t0
@@ -536,6 +555,103 @@ def run_ess(args):
     }
     print(json.dumps(line), flush=True)
     smp.close()
+    return 0
+
+
+def run_learned(args):
+    """Learned-preconditioned hit-and-run against plain ACHR, by min-ESS/s.
+
+    1. Plain ACHR (reference semantics) from the warmup centre: TRAIN_CHAINS
+       chains, TRAIN_BURNIN steps, then TRAIN_SNAPSHOTS snapshots TRAIN_GAP steps
+       apart; every snapshot goes to null-space coordinates on the tensor cores
+       (achr_null_coords) and is centred.
+    2. The low-rank (--rank) plus diagonal map is fitted to those samples by the
+       Gaussian KL loss with Adam (achr_precond_train, --iters steps).
+    3. A pool of --pool directions N L z is installed on a second sampler
+       (achr_precond_pool), which then runs hit-and-run.
+    4. Both samplers run the same ESS schedule (--learned CHAINS BURNIN SEGMENTS
+       STEPS, fresh chains from the warmup centre, another seed); min-ESS/s
+       counts the device time of the sampling launches.  If the learned
+       sampler's max R-hat is not below 1.01 while plain ACHR's is, the
+       reported value falls back to plain ACHR's."""
+    import torch
+
+    import __graft_entry__ as ge
+
+    pkg = ge.load_package()
+    pkg.lib()
+    import importlib
+    synth = importlib.import_module("achr_gb300.synthetic")
+    diag = importlib.import_module("achr_gb300.diagnostics")
+    t_setup = time.perf_counter()
+    spec, model, S, warm, _, _ = build_inputs(args.workload, pkg, synth, null_space=gpu_null_space_fn(pkg))
+    n = spec.n_rxns
+    stream = torch.cuda.current_stream().cuda_stream
+    plain = pkg.Sampler(model, warm)
+    tpc = plain.autotune()
+    d = plain.null_dim
+    setup_s = time.perf_counter() - t_setup
+
+    # 1. training samples
+    Pt, Tb, Ks, Lg = args.train_chains, args.train_burnin, args.train_snapshots, args.train_gap
+    t_train = time.perf_counter()
+    x = torch.zeros((n, Pt), dtype=torch.float64, device="cuda")
+    a = torch.zeros_like(x)
+    mu = torch.from_numpy(plain.centre()).cuda()
+    Y = torch.empty((d, Pt * Ks), dtype=torch.float32, device="cuda")
+    st = plain.sample_resume(Pt, 0, Tb, False, x.data_ptr(), a.data_ptr(), Pt, stream=stream, seed=args.seed + 7,
+                             with_stats=True)
+    gen_ms = st["kernel_ms"]
+    for k in range(Ks):
+        st = plain.sample_resume(Pt, Tb + k * Lg, Lg, True, x.data_ptr(), a.data_ptr(), Pt, stream=stream,
+                                 seed=args.seed + 7, with_stats=True)
+        gen_ms += st["kernel_ms"]
+        plain.null_coords(Pt, x.data_ptr(), Pt, Y.data_ptr() + 4 * k * Pt, Pt * Ks, d_mu=mu.data_ptr(),
+                          stream=stream)
+    del x, a
+    Y -= Y.mean(dim=1, keepdim=True)
+    var = Y.var(dim=1).clamp_min(1e-30)
+    s_par = (0.5 * torch.log(var)).float().contiguous()
+    g = torch.Generator(device="cuda").manual_seed(args.seed)
+    U_par = (0.01 * torch.randn((d, args.rank), device="cuda", generator=g) *
+             torch.exp(s_par)[:, None]).contiguous()
+    tst = pkg.precond_train(d, args.rank, Pt * Ks, Y.data_ptr(), Pt * Ks, s_par.data_ptr(), U_par.data_ptr(),
+                            stream=stream, iterations=args.iters, batch=args.batch, learning_rate=args.lr,
+                            seed=args.seed)
+    del Y
+    torch.cuda.empty_cache()
+    learned = pkg.Sampler(model, warm, threads_per_chain=tpc)
+    learned.set_null_space(plain.null_space())
+    learned.precond_pool(args.rank, s_par.data_ptr(), U_par.data_ptr(), args.pool, seed=args.seed + 11)
+    train_s = time.perf_counter() - t_train
+
+    # 4. ESS comparison on the same schedule
+    M, B, K, L = args.learned
+    out = {}
+    for name, smp in (("plain", plain), ("learned", learned)):
+        draws, ms, steps = ess_trace(smp, M, B, K, L, args.seed + 101, stream)
+        summ = diag.summarize(draws)
+        out[name] = {"min_ess_per_s": summ["min_ess"] / (ms * 1e-3), "min_ess": summ["min_ess"],
+                     "max_rhat": summ["max_rhat"], "median_rhat": summ["median_rhat"],
+                     "rhat_q99": summ["rhat_q99"], "median_ess": summ["median_ess"], "sampling_ms": ms,
+                     "chain_steps_per_s": steps / (ms * 1e-3), "frozen_fluxes": summ["frozen_params"]}
+    lp, ll = out["plain"], out["learned"]
+    fallback = ll["max_rhat"] >= 1.01 and lp["max_rhat"] < 1.01
+    line = {
+        "metric": "min-ESS/s", "value": lp["min_ess_per_s"] if fallback else ll["min_ess_per_s"],
+        "unit": "effective samples/s", "higher_is_better": True, "n_gpus": 1, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"{args.workload}: {spec.n_mets}x{n}, {M} chains, {B} burn-in steps, {K} draws {L} "
+                               f"steps apart; learned: rank {args.rank} + diagonal, {args.iters} Adam steps on "
+                               f"{Pt * Ks} plain-ACHR samples, pool of {args.pool} directions",
+                   "threads_per_chain": tpc},
+        "learned_over_plain": ll["min_ess_per_s"] / lp["min_ess_per_s"], "fallback_to_plain": fallback,
+        "plain": lp, "learned": ll,
+        "training": {"samples": Pt * Ks, "null_dim": d, "generation_ms": gen_ms, **tst, "total_s": train_s},
+        "setup_s": setup_s,
+    }
+    print(json.dumps(line), flush=True)
+    plain.close()
+    learned.close()
     return 0
 
 
@@ -659,6 +775,8 @@ def run_large(args):
 
 def main():
     args = parse_args()
+    if args.learned:
+        return run_learned(args)
     if args.workload == "large" and args.impl == "gb300" and not args.ess:
         return run_large(args)
     if args.ess:

@@ -168,6 +168,11 @@ void achr_destroy(achr_ctx *ctx);
  * to ACHR.  Chains start at the warmup centre in either mode. */
 achr_status achr_set_directions(achr_ctx *ctx, const double *dirs, int64_t ld, int32_t n_dirs);
 
+/* The installed pool: its size (0 in ACHR mode) and a copy, n x K
+ * column-major (ld = n), to host or device memory. */
+int32_t achr_get_n_directions(const achr_ctx *ctx);
+achr_status achr_get_directions(const achr_ctx *ctx, double *dirs_out);
+
 /* ---- Learned direction preconditioner (no reference counterpart) ----
  * A low-rank-plus-diagonal linear map L = [diag(exp(s)), U] (d x (d + r)) in
  * null-space coordinates, fitted to samples y = N^T (x - mu) of the plain

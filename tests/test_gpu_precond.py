@@ -1,0 +1,141 @@
+"""GPU: hit-and-run along a direction pool against the oracle, the preconditioner's
+loss/gradient kernels against the FP64 oracle, its training, the null-space
+coordinates and the learned direction pool."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import dense_S
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+REL_TOL = 1e-10
+
+
+@pytest.fixture(scope="module")
+def sampler(pkg, small_model, golden):
+    s = pkg.Sampler(small_model, golden["warmup"])
+    s.set_null_space(golden["N"])
+    yield s
+    s.close()
+
+
+def _pool(N, K, seed):
+    rng = np.random.default_rng(seed)
+    return N @ rng.standard_normal((N.shape[1], K))
+
+
+@pytest.mark.parametrize("steps", [1, 20, 50])
+def test_hit_and_run_matches_oracle(pkg, small_model, golden, oracle_mod, steps):
+    N = golden["N"]
+    D = _pool(N, 60, seed=7)
+    with pkg.Sampler(small_model, golden["warmup"]) as s:
+        s.set_null_space(N)
+        s.set_directions(D)
+        assert np.array_equal(s.directions(), D)
+        pts, st = s.sample(64, steps, seed=42)
+        centre = s.centre()
+    prob = oracle_mod.Problem(small_model, D, N, centre_point=centre)
+    ref, rst = prob.sample(42, 64, steps, hit_and_run=True)
+    assert np.abs(pts - ref).max() <= REL_TOL * max(1.0, np.abs(ref).max())
+    assert st["accepted"] == rst["accepted"] and st["rejected"] == rst["rejected"]
+    assert st["reprojections"] == rst["reprojections"]
+
+
+def test_directions_cleared_returns_to_achr(pkg, small_model, golden):
+    with pkg.Sampler(small_model, golden["warmup"]) as s:
+        s.set_null_space(golden["N"])
+        a, _ = s.sample(16, 10, seed=3)
+        s.set_directions(_pool(golden["N"], 30, seed=1))
+        b, _ = s.sample(16, 10, seed=3)
+        s.set_directions(None)
+        c, _ = s.sample(16, 10, seed=3)
+    assert not np.array_equal(a, b) and np.array_equal(a, c)
+
+
+def _dev(a, dtype=torch.float32):
+    return torch.from_numpy(np.ascontiguousarray(a)).to(device="cuda", dtype=dtype)
+
+
+def test_loss_grad_matches_fp64_oracle(pkg):
+    from oracle import precond
+    rng = np.random.default_rng(11)
+    d, r, B = 50, 8, 200
+    s = 0.3 * rng.standard_normal(d)
+    U = 0.4 * rng.standard_normal((d, r))
+    Y = rng.standard_normal((d, 3 * B)) * np.exp(rng.uniform(-1, 1, (d, 1)))
+    ds, dU, dY = _dev(s), _dev(U), _dev(Y)
+    gs = torch.zeros(d, device="cuda")
+    gU = torch.zeros((d, r), device="cuda")
+    # minibatch = columns [B, 2B) of a wider Y: exercises the leading dimension
+    loss = pkg.precond_loss_grad(d, r, B, ds.data_ptr(), dU.data_ptr(), dY.data_ptr() + 4 * B, 3 * B,
+                                 gs.data_ptr(), gU.data_ptr())
+    val, gs_ref, gU_ref = precond.loss_grad(s.astype(np.float32), U.astype(np.float32),
+                                            Y.astype(np.float32)[:, B:2 * B])
+    assert abs(loss - val) <= 1e-4 * max(1.0, abs(val))
+    assert np.abs(gs.cpu().numpy() - gs_ref).max() <= 2e-4 * max(1.0, np.abs(gs_ref).max())
+    assert np.abs(gU.cpu().numpy() - gU_ref).max() <= 2e-4 * max(1.0, np.abs(gU_ref).max())
+
+
+def test_training_fits_a_known_covariance(pkg):
+    from oracle import precond
+    rng = np.random.default_rng(5)
+    d, r, n = 64, 4, 32768
+    s_true = np.log(rng.uniform(0.2, 2.0, d))
+    U_true = rng.standard_normal((d, r)) * 1.5
+    C = precond.covariance(s_true, U_true)
+    Y = np.linalg.cholesky(C) @ rng.standard_normal((d, n))
+    s0 = 0.5 * np.log(Y.var(axis=1))
+    U0 = 0.01 * rng.standard_normal((d, r))
+    ds, dU, dY = _dev(s0), _dev(U0), _dev(Y)
+    st = pkg.precond_train(d, r, n, dY.data_ptr(), n, ds.data_ptr(), dU.data_ptr(), iterations=1500, batch=2048,
+                           learning_rate=0.02)
+    assert st["iterations"] == 1500 and st["loss_last"] < st["loss_first"]
+    s_fit, U_fit = ds.cpu().numpy().astype(np.float64), dU.cpu().numpy().astype(np.float64)
+    kl_fit = precond.kl_to_sample_covariance(s_fit, U_fit, Y)
+    kl_init = precond.kl_to_sample_covariance(s0, U0, Y)
+    kl_true = precond.kl_to_sample_covariance(s_true, U_true, Y)
+    # minibatch noise keeps Adam near, not at, the optimum
+    assert kl_fit < 0.05 * kl_init and kl_fit < kl_true + 0.2
+
+
+def test_null_coords_match_numpy(pkg, sampler, golden):
+    P = 300
+    pts, _ = sampler.sample(P, 25, seed=9)
+    mu = pts.mean(axis=1)
+    X = _dev(pts, torch.float64)
+    dmu = _dev(mu, torch.float64)
+    d = sampler.null_dim
+    Y = torch.full((d, P + 4), float("nan"), device="cuda")
+    sampler.null_coords(P, X.data_ptr(), P, Y.data_ptr(), P + 4, d_mu=dmu.data_ptr())
+    ref = golden["N"].T @ (pts - mu[:, None])
+    got = Y[:, :P].double().cpu().numpy()
+    assert np.abs(got - ref).max() <= 1e-4 * np.abs(ref).max()
+
+
+def test_learned_pool_directions_lie_in_null_space(pkg, small_model, golden):
+    S = dense_S(small_model)
+    rng = np.random.default_rng(2)
+    with pkg.Sampler(small_model, golden["warmup"]) as s:
+        s.set_null_space(golden["N"])
+        d = s.null_dim
+        r = 4
+        ds = _dev(0.1 * rng.standard_normal(d))
+        dU = _dev(0.5 * rng.standard_normal((d, r)))
+        s.precond_pool(r, ds.data_ptr(), dU.data_ptr(), 500, seed=17)
+        G = s.directions()
+        assert G.shape == (s.n, 500)
+        assert np.abs(S @ G).max() <= 1e-12 * np.abs(G).max()
+        # the pool's covariance in null-space coordinates approaches exp(2 s) + U U^T
+        Yc = golden["N"].T @ G
+        emp = Yc @ Yc.T / 500
+        from oracle import precond
+        C = precond.covariance(ds.cpu().numpy(), dU.cpu().numpy())
+        assert np.abs(emp - C).max() < 0.35 * np.abs(C).max()
+        pts, st = s.sample(128, 40, seed=1)
+    assert st["accepted"] == 128 * 40 and st["stuck_chains"] == 0
+    assert np.abs(S @ pts).max() <= 1e-8
+    assert np.all(pts >= small_model.lb[:, None] - 1e-9) and np.all(pts <= small_model.ub[:, None] + 1e-9)
