@@ -62,7 +62,7 @@ def parse_args():
     ap.add_argument("--train-burnin", type=int, default=2000)
     ap.add_argument("--train-snapshots", type=int, default=8)
     ap.add_argument("--train-gap", type=int, default=250)
-    ap.add_argument("--rank", type=int, default=256)
+    ap.add_argument("--precond-rank", type=int, default=256, help="rank of the learned preconditioner")
     ap.add_argument("--iters", type=int, default=2000)
     ap.add_argument("--batch", type=int, default=4096)
     ap.add_argument("--lr", type=float, default=0.01)
@@ -270,7 +270,8 @@ def run_gpu(args):
     synth = importlib.import_module("achr_gb300.synthetic")
     spec, model, S, warm, P, T = build_inputs(args.workload, pkg, synth)
     n = spec.n_rxns
-    chain_base = rank * P  # weak scaling: every rank runs its own P chains
+    sharding = importlib.import_module("achr_gb300.sharding")
+    chain_base, _ = sharding.chain_block(rank, world, P)  # weak scaling: every rank runs its own P chains
 
     t_setup = time.perf_counter()
     smp = pkg.Sampler(model, warm)
@@ -301,9 +302,7 @@ def run_gpu(args):
     per_launch = [evs[k].elapsed_time(evs[k + 1]) for k in range(args.steps)]
     ms = sum(per_launch) / args.steps
     if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+        ms = sharding.max_over_ranks(ms, device="cuda")
         torch.distributed.barrier()
     chain_steps = P * T
     value = world * chain_steps / (ms * 1e-3)
@@ -565,7 +564,7 @@ def run_learned(args):
        chains, TRAIN_BURNIN steps, then TRAIN_SNAPSHOTS snapshots TRAIN_GAP steps
        apart; every snapshot goes to null-space coordinates on the tensor cores
        (achr_null_coords) and is centred.
-    2. The low-rank (--rank) plus diagonal map is fitted to those samples by the
+    2. The low-rank (--precond-rank) plus diagonal map is fitted to those samples by the
        Gaussian KL loss with Adam (achr_precond_train, --iters steps).
     3. A pool of --pool directions N L z is installed on a second sampler
        (achr_precond_pool), which then runs hit-and-run.
@@ -613,16 +612,16 @@ def run_learned(args):
     var = Y.var(dim=1).clamp_min(1e-30)
     s_par = (0.5 * torch.log(var)).float().contiguous()
     g = torch.Generator(device="cuda").manual_seed(args.seed)
-    U_par = (0.01 * torch.randn((d, args.rank), device="cuda", generator=g) *
+    U_par = (0.01 * torch.randn((d, args.precond_rank), device="cuda", generator=g) *
              torch.exp(s_par)[:, None]).contiguous()
-    tst = pkg.precond_train(d, args.rank, Pt * Ks, Y.data_ptr(), Pt * Ks, s_par.data_ptr(), U_par.data_ptr(),
+    tst = pkg.precond_train(d, args.precond_rank, Pt * Ks, Y.data_ptr(), Pt * Ks, s_par.data_ptr(), U_par.data_ptr(),
                             stream=stream, iterations=args.iters, batch=args.batch, learning_rate=args.lr,
                             seed=args.seed)
     del Y
     torch.cuda.empty_cache()
     learned = pkg.Sampler(model, warm, threads_per_chain=tpc)
     learned.set_null_space(plain.null_space())
-    learned.precond_pool(args.rank, s_par.data_ptr(), U_par.data_ptr(), args.pool, seed=args.seed + 11)
+    learned.precond_pool(args.precond_rank, s_par.data_ptr(), U_par.data_ptr(), args.pool, seed=args.seed + 11)
     train_s = time.perf_counter() - t_train
 
     # 4. ESS comparison on the same schedule
@@ -641,7 +640,7 @@ def run_learned(args):
         "metric": "min-ESS/s", "value": lp["min_ess_per_s"] if fallback else ll["min_ess_per_s"],
         "unit": "effective samples/s", "higher_is_better": True, "n_gpus": 1, "dtype": "f64", "data": "synthetic",
         "config": {"workload": f"{args.workload}: {spec.n_mets}x{n}, {M} chains, {B} burn-in steps, {K} draws {L} "
-                               f"steps apart; learned: rank {args.rank} + diagonal, {args.iters} Adam steps on "
+                               f"steps apart; learned: rank {args.precond_rank} + diagonal, {args.iters} Adam steps on "
                                f"{Pt * Ks} plain-ACHR samples, pool of {args.pool} directions",
                    "threads_per_chain": tpc},
         "learned_over_plain": ll["min_ess_per_s"] / lp["min_ess_per_s"], "fallback_to_plain": fallback,
