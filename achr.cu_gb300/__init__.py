@@ -154,6 +154,8 @@ _SIGNATURES = {
     "achr_get_n_directions": (C.c_int32, [C.c_void_p]),
     "achr_get_directions": (C.c_int, [C.c_void_p, C.c_void_p]),
     "achr_precond_default_options": (None, [C.POINTER(PrecondOptions)]),
+    "achr_precond_dim": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
+    "achr_get_precond_basis": (C.c_int, [C.c_void_p, C.c_void_p]),
     "achr_null_coords": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_int64,
                                    C.c_void_p]),
     "achr_precond_loss_grad": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p,
@@ -402,6 +404,19 @@ class Sampler:
         out = np.zeros((self.n, k), order="F")
         if k:
             _check(lib().achr_get_directions(self._ctx, out.ctypes.data_as(C.c_void_p)))
+        return out
+
+    def precond_dim(self) -> tuple[int, int]:
+        """(dimension of the preconditioner's basis, reactions pinned across all warmup points)."""
+        d, f = C.c_int32(), C.c_int32()
+        _check(lib().achr_precond_dim(self._ctx, C.byref(d), C.byref(f)))
+        return d.value, f.value
+
+    def precond_basis(self) -> np.ndarray:
+        d, _ = self.precond_dim()
+        out = np.zeros((self.n, d), order="F")
+        if d:
+            _check(lib().achr_get_precond_basis(self._ctx, out.ctypes.data_as(C.c_void_p)))
         return out
 
     def null_coords(self, n_points: int, d_points: int, ld: int, d_Y: int, ldy: int, d_mu: int = 0,

@@ -62,4 +62,9 @@ struct achr_ctx {
     achr::DevBuf<double> dirs;   // hit-and-run direction pool, n x n_dirs (leading dimension ldw)
     int n_dirs = 0;              // 0: ACHR directions (warmup point minus centre)
     achr::DevBuf<double> zeros;  // np zeros: the (unused) centre accumulator of hit-and-run chains
+    // Basis of the directions the polytope spans: the null space of S with the
+    // reactions that are fixed across all warmup points also held fixed
+    // (n x d_act, column-major); built on first use by the preconditioner.
+    achr::DevBuf<double> Nact;
+    int d_act = -1, n_frozen = 0;
 };

@@ -1,5 +1,6 @@
 // Learned direction preconditioner: a low-rank-plus-diagonal linear map in
-// null-space coordinates, fitted on the GPU to samples of the plain sampler,
+// the coordinates of the directions the polytope spans (the null space of S
+// with the reactions pinned in every warmup point held fixed), fitted on the GPU to samples of the plain sampler,
 // and the pool of hit-and-run directions it generates.  No reference
 // counterpart (the reference's only direction rule is ACHR's, ACHRcu/
 // ACHRCuda.cu:260-264).
@@ -18,6 +19,7 @@
 // Every step is a kernel of this file: FP32 tiled GEMMs, a single-CTA
 // Cholesky factorisation and inverse of M, row reductions, Adam.
 #include <cublas_v2.h>
+#include <cusolverDn.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -315,6 +317,100 @@ __global__ void __launch_bounds__(kSplitWarps * 32)
 
 unsigned blocks_for(long long n, int t = 256) { return (unsigned)((n + t - 1) / t); }
 
+// Reactions whose value is the same in every warmup point (to 1e-9 relative):
+// implicit equalities of the polytope (blocked or pinned fluxes).  One thread
+// per reaction, coalesced over reactions.
+__global__ void frozen_kernel(int n, int W, int ldw, const double *__restrict__ warmup, int *__restrict__ frozen) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double lo = INFINITY, hi = -INFINITY;
+    for (int j = 0; j < W; ++j) {
+        const double v = warmup[(long long)j * ldw + i];
+        lo = fmin(lo, v);
+        hi = fmax(hi, v);
+    }
+    frozen[i] = (hi - lo) <= 1e-9 * fmax(1.0, fmax(fabs(lo), fabs(hi))) ? 1 : 0;
+}
+
+__global__ void add_diag_kernel(int n, const int *__restrict__ frozen, double *__restrict__ G) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n && frozen[i]) G[(long long)i * n + i] += 1.0;
+}
+
+// The basis the preconditioner works in: null space of [S; E], E the unit rows
+// of the frozen reactions, by the reference's eigenvalue rule on
+// S^T S + E^T E (ACHRCuda.cu:436-502 applied to the stacked matrix).
+achr_status ensure_active_basis(achr_ctx *ctx) {
+    if (ctx->d_act >= 0) return ACHR_OK;
+    const int n = ctx->n, m = ctx->m;
+    DevBuf<int> frozen, info;
+    PC_TRY(frozen.alloc(n));
+    frozen_kernel<<<blocks_for(n), 256>>>(n, ctx->W, ctx->ldw, ctx->warmup.p, frozen.p);
+    PC_TRY(cudaGetLastError());
+    std::vector<int> hf((size_t)n);
+    PC_TRY(cudaMemcpy(hf.data(), frozen.p, sizeof(int) * n, cudaMemcpyDeviceToHost));
+    int nf = 0;
+    for (int v : hf) nf += v;
+    if (nf == 0) {  // nothing pinned: the null space itself
+        PC_TRY(ctx->Nact.alloc((size_t)n * std::max(ctx->d, 1)));
+        if (ctx->d > 0)
+            PC_TRY(cudaMemcpy(ctx->Nact.p, ctx->N.p, sizeof(double) * (size_t)n * ctx->d, cudaMemcpyDeviceToDevice));
+        ctx->d_act = ctx->d;
+        ctx->n_frozen = 0;
+        return ACHR_OK;
+    }
+    std::vector<double> dS((size_t)m * n, 0.0);
+    for (int i = 0; i < m; ++i)
+        for (int q = ctx->h_rowptr[(size_t)i]; q < ctx->h_rowptr[(size_t)i + 1]; ++q)
+            dS[(size_t)ctx->h_colidx[(size_t)q] * m + i] = ctx->h_val[(size_t)q];
+    DevBuf<double> S, G, lam, work;
+    PC_TRY(S.upload(dS.data(), dS.size()));
+    PC_TRY(G.alloc((size_t)n * n));
+    PC_TRY(lam.alloc(n));
+    PC_TRY(info.alloc(1));
+    cublasHandle_t cb = nullptr;
+    if (cublasCreate(&cb) != CUBLAS_STATUS_SUCCESS) return pc_err(ACHR_ERR_CUDA, "cublasCreate failed");
+    const double one = 1.0, zero = 0.0;
+    const cublasStatus_t bs =
+        m > 0 ? cublasDgemm(cb, CUBLAS_OP_T, CUBLAS_OP_N, n, n, m, &one, S.p, m, S.p, m, &zero, G.p, n)
+              : CUBLAS_STATUS_SUCCESS;
+    cublasDestroy(cb);
+    if (bs != CUBLAS_STATUS_SUCCESS) return pc_err(ACHR_ERR_CUDA, "cublasDgemm (S^T S) failed");
+    if (m == 0) PC_TRY(cudaMemset(G.p, 0, sizeof(double) * (size_t)n * n));
+    add_diag_kernel<<<blocks_for(n), 256>>>(n, frozen.p, G.p);
+    PC_TRY(cudaGetLastError());
+    cusolverDnHandle_t sh = nullptr;
+    if (cusolverDnCreate(&sh) != CUSOLVER_STATUS_SUCCESS) return pc_err(ACHR_ERR_CUDA, "cusolverDnCreate failed");
+    int lwork = 0;
+    cusolverStatus_t ss =
+        cusolverDnDsyevd_bufferSize(sh, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n, G.p, n, lam.p, &lwork);
+    if (ss == CUSOLVER_STATUS_SUCCESS) {
+        if (cudaError_t e = work.alloc((size_t)std::max(lwork, 1))) {
+            cusolverDnDestroy(sh);
+            return pc_err(ACHR_ERR_CUDA, std::string("syevd workspace: ") + cudaGetErrorString(e));
+        }
+        ss = cusolverDnDsyevd(sh, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n, G.p, n, lam.p, work.p, lwork,
+                              info.p);
+    }
+    cusolverDnDestroy(sh);
+    if (ss != CUSOLVER_STATUS_SUCCESS) return pc_err(ACHR_ERR_NUMERIC, "cusolverDnDsyevd (active basis) failed");
+    int h_info = 0;
+    PC_TRY(cudaMemcpy(&h_info, info.p, sizeof(int), cudaMemcpyDeviceToHost));
+    if (h_info != 0) return pc_err(ACHR_ERR_NUMERIC, "syevd (active basis) did not converge");
+    std::vector<double> hl((size_t)n);
+    PC_TRY(cudaMemcpy(hl.data(), lam.p, sizeof(double) * n, cudaMemcpyDeviceToHost));
+    double smax = 0.0;
+    for (double v : hl) smax = std::max(smax, std::fabs(v));
+    const double tol = (double)n * smax * 2.2204e-16;
+    int d = 0;  // eigenvalues ascend: the basis is the leading block of columns
+    while (d < n && std::fabs(hl[(size_t)d]) < tol) ++d;
+    PC_TRY(ctx->Nact.alloc((size_t)n * std::max(d, 1)));
+    if (d > 0) PC_TRY(cudaMemcpy(ctx->Nact.p, G.p, sizeof(double) * (size_t)n * d, cudaMemcpyDeviceToDevice));
+    ctx->d_act = d;
+    ctx->n_frozen = nf;
+    return ACHR_OK;
+}
+
 // Device workspace of one loss/gradient evaluation.
 struct PcWork {
     DevBuf<float> a, W, M, Lw, Xw, Minv, Q, Rq, V, K, T, yv, scal;  // scal: [0] logdet, [1] loss
@@ -483,13 +579,35 @@ achr_status achr_precond_train(int32_t d, int32_t r, int32_t n_samples, const fl
     return ACHR_OK;
 }
 
+achr_status achr_precond_dim(achr_ctx *ctx, int32_t *d_out, int32_t *n_frozen_out) {
+    using namespace achr;
+    if (!ctx) return pc_err(ACHR_ERR_INVALID, "ctx is NULL");
+    achr_status st = ensure_active_basis(ctx);
+    if (st != ACHR_OK) return st;
+    if (d_out) *d_out = ctx->d_act;
+    if (n_frozen_out) *n_frozen_out = ctx->n_frozen;
+    return ACHR_OK;
+}
+
+achr_status achr_get_precond_basis(achr_ctx *ctx, double *basis_out) {
+    using namespace achr;
+    if (!ctx || !basis_out) return pc_err(ACHR_ERR_INVALID, "NULL argument");
+    achr_status st = ensure_active_basis(ctx);
+    if (st != ACHR_OK) return st;
+    if (ctx->d_act > 0)
+        PC_TRY(cudaMemcpy(basis_out, ctx->Nact.p, sizeof(double) * (size_t)ctx->n * ctx->d_act, cudaMemcpyDefault));
+    return ACHR_OK;
+}
+
 achr_status achr_null_coords(achr_ctx *ctx, int32_t n_points, const double *d_points, int64_t ld, const double *d_mu,
                              float *d_Y, int64_t ldy, void *stream) {
     using namespace achr;
     if (!ctx || n_points < 0 || (n_points > 0 && (!d_points || !d_Y)) || ld < n_points || ldy < n_points)
         return pc_err(ACHR_ERR_INVALID, "bad null-coordinate arguments");
-    if (n_points == 0 || ctx->d == 0) return ACHR_OK;
-    const int n = ctx->n, d = ctx->d, kpad = (n + 63) / 64 * 64;
+    achr_status bst = ensure_active_basis(ctx);
+    if (bst != ACHR_OK) return bst;
+    if (n_points == 0 || ctx->d_act == 0) return ACHR_OK;
+    const int n = ctx->n, d = ctx->d_act, kpad = (n + 63) / 64 * 64;
     cudaStream_t st = (cudaStream_t)stream;
     DevBuf<__nv_bfloat16> Nh, Nl, Xh, Xl;
     DevBuf<unsigned long long> err;
@@ -497,7 +615,7 @@ achr_status achr_null_coords(achr_ctx *ctx, int32_t n_points, const double *d_po
     PC_TRY(Nl.alloc((size_t)d * kpad));
     PC_TRY(err.alloc(1));
     PC_TRY(cudaMemsetAsync(err.p, 0, sizeof(unsigned long long), st));
-    split_nt_kernel<<<blocks_for((long long)d * kpad), 256, 0, st>>>(n, d, kpad, ctx->N.p, Nh.p, Nl.p);
+    split_nt_kernel<<<blocks_for((long long)d * kpad), 256, 0, st>>>(n, d, kpad, ctx->Nact.p, Nh.p, Nl.p);
     PC_TRY(cudaGetLastError());
     const int chunk = std::min(n_points, 65536);
     PC_TRY(Xh.alloc((size_t)chunk * kpad));
@@ -523,8 +641,10 @@ achr_status achr_precond_pool(achr_ctx *ctx, int32_t r, const float *d_s, const 
                               uint64_t seed) {
     using namespace achr;
     if (!ctx || r < 0 || !d_s || (r > 0 && !d_U) || n_dirs <= 0) return pc_err(ACHR_ERR_INVALID, "bad pool arguments");
-    const int n = ctx->n, d = ctx->d, K = n_dirs;
-    if (d == 0) return pc_err(ACHR_ERR_UNSUPPORTED, "null space is empty");
+    achr_status bst = ensure_active_basis(ctx);
+    if (bst != ACHR_OK) return bst;
+    const int n = ctx->n, d = ctx->d_act, K = n_dirs;
+    if (d == 0) return pc_err(ACHR_ERR_UNSUPPORTED, "the polytope spans no direction");
     DevBuf<float> Yp, Z2;
     DevBuf<double> Yd, G;
     PC_TRY(Yp.alloc((size_t)d * K));
@@ -546,7 +666,7 @@ achr_status achr_precond_pool(achr_ctx *ctx, int32_t r, const float *d_s, const 
     if (cublasCreate(&cb) != CUBLAS_STATUS_SUCCESS) return pc_err(ACHR_ERR_CUDA, "cublasCreate failed");
     const double one = 1.0, zero = 0.0;
     const cublasStatus_t bs =
-        cublasDgemm(cb, CUBLAS_OP_N, CUBLAS_OP_T, n, K, d, &one, ctx->N.p, n, Yd.p, K, &zero, G.p, ctx->ldw);
+        cublasDgemm(cb, CUBLAS_OP_N, CUBLAS_OP_T, n, K, d, &one, ctx->Nact.p, n, Yd.p, K, &zero, G.p, ctx->ldw);
     cublasDestroy(cb);
     if (bs != CUBLAS_STATUS_SUCCESS) return pc_err(ACHR_ERR_CUDA, "cublasDgemm (direction pool) failed");
     PC_TRY(cudaDeviceSynchronize());

@@ -56,6 +56,7 @@ def parse_args():
     ap.add_argument("--ess", type=int, nargs=4, metavar=("CHAINS", "BURNIN", "SEGMENTS", "STEPS"),
                     help="min-ESS/s and max R-hat from trace snapshots: CHAINS chains, BURNIN steps, then SEGMENTS "
                          "snapshots STEPS steps apart")
+    ap.add_argument("--gemm", type=int, metavar="CHAINS", help="time the tensor-core GEMM alone at this N")
     ap.add_argument("--learned", type=int, nargs=4, metavar=("CHAINS", "BURNIN", "SEGMENTS", "STEPS"),
                     help="learned-preconditioned hit-and-run against plain ACHR on this ESS schedule")
     ap.add_argument("--train-chains", type=int, default=65536)
@@ -566,8 +567,9 @@ def run_learned(args):
        (achr_null_coords) and is centred.
     2. The low-rank (--precond-rank) plus diagonal map is fitted to those samples by the
        Gaussian KL loss with Adam (achr_precond_train, --iters steps).
-    3. A pool of --pool directions N L z is installed on a second sampler
-       (achr_precond_pool), which then runs hit-and-run.
+    3. A pool of --pool directions B L z (B: the basis of the directions the
+       polytope spans) is installed (achr_precond_pool); the sampler then runs
+       hit-and-run.
     4. Both samplers run the same ESS schedule (--learned CHAINS BURNIN SEGMENTS
        STEPS, fresh chains from the warmup centre, another seed); min-ESS/s
        counts the device time of the sampling launches.  If the learned
@@ -588,7 +590,8 @@ def run_learned(args):
     stream = torch.cuda.current_stream().cuda_stream
     plain = pkg.Sampler(model, warm)
     tpc = plain.autotune()
-    d = plain.null_dim
+    d, n_frozen = plain.precond_dim()  # directions the polytope spans (pinned reactions held fixed)
+    null_dim = plain.null_dim
     setup_s = time.perf_counter() - t_setup
 
     # 1. training samples
@@ -619,16 +622,16 @@ def run_learned(args):
                             seed=args.seed)
     del Y
     torch.cuda.empty_cache()
-    learned = pkg.Sampler(model, warm, threads_per_chain=tpc)
-    learned.set_null_space(plain.null_space())
-    learned.precond_pool(args.precond_rank, s_par.data_ptr(), U_par.data_ptr(), args.pool, seed=args.seed + 11)
     train_s = time.perf_counter() - t_train
 
-    # 4. ESS comparison on the same schedule
+    # 4. ESS comparison on the same schedule; the same context switches to the
+    # learned pool after the plain run, so both use the same basis.
     M, B, K, L = args.learned
     out = {}
-    for name, smp in (("plain", plain), ("learned", learned)):
-        draws, ms, steps = ess_trace(smp, M, B, K, L, args.seed + 101, stream)
+    for name in ("plain", "learned"):
+        if name == "learned":
+            plain.precond_pool(args.precond_rank, s_par.data_ptr(), U_par.data_ptr(), args.pool, seed=args.seed + 11)
+        draws, ms, steps = ess_trace(plain, M, B, K, L, args.seed + 101, stream)
         summ = diag.summarize(draws)
         out[name] = {"min_ess_per_s": summ["min_ess"] / (ms * 1e-3), "min_ess": summ["min_ess"],
                      "max_rhat": summ["max_rhat"], "median_rhat": summ["median_rhat"],
@@ -645,12 +648,12 @@ def run_learned(args):
                    "threads_per_chain": tpc},
         "learned_over_plain": ll["min_ess_per_s"] / lp["min_ess_per_s"], "fallback_to_plain": fallback,
         "plain": lp, "learned": ll,
-        "training": {"samples": Pt * Ks, "null_dim": d, "generation_ms": gen_ms, **tst, "total_s": train_s},
+        "training": {"samples": Pt * Ks, "basis_dim": d, "null_dim": null_dim, "pinned_reactions": n_frozen,
+                     "generation_ms": gen_ms, **tst, "total_s": train_s},
         "setup_s": setup_s,
     }
     print(json.dumps(line), flush=True)
     plain.close()
-    learned.close()
     return 0
 
 
@@ -772,8 +775,53 @@ def run_large(args):
     return 0
 
 
+def run_gemm(args):
+    """The tensor-core GEMM alone on the reprojection's shape: M = 5063 (metabolites of
+    the large model), K = 5120 (padded), N = --gemm CHAINS, one product and the three
+    split products; CUDA-event timing over 5 calls after 2 warm-up calls."""
+    import torch
+
+    import __graft_entry__ as ge
+
+    pkg = ge.load_package()
+    m, kpad, N = 5063, 5120, args.gemm
+    g = torch.Generator(device="cuda").manual_seed(args.seed)
+    A0 = torch.randn(m, kpad, device="cuda", generator=g).to(torch.bfloat16)
+    A1 = (torch.randn(m, kpad, device="cuda", generator=g) * 2.0 ** -9).to(torch.bfloat16)
+    B0 = torch.randn(N, kpad, device="cuda", generator=g).to(torch.bfloat16)
+    B1 = (torch.randn(N, kpad, device="cuda", generator=g) * 2.0 ** -9).to(torch.bfloat16)
+    C = torch.empty(m, N, device="cuda", dtype=torch.float32)
+    tpeak, tpeak_kind = load_tensor_peak()
+    rows = {}
+    for nsplit in (1, 3):
+        a1 = A1.data_ptr() if nsplit == 3 else 0
+        b1 = B1.data_ptr() if nsplit == 3 else 0
+        call = lambda: pkg.gemm_bf16(m, N, kpad, A0.data_ptr(), B0.data_ptr(), C.data_ptr(), kpad, kpad, N,  # noqa: E731
+                                     A1=a1, B1=b1)
+        for _ in range(2):
+            call()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(5):
+            call()
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / 5
+        tf = 2.0 * m * N * kpad * nsplit / (ms * 1e-3) / 1e12
+        rows[f"nsplit{nsplit}"] = {"ms": ms, "tflops": tf, "tensor_frac": tf / tpeak}
+    line = {"metric": "TFLOP/s", "value": rows["nsplit3"]["tflops"], "unit": "TFLOP/s", "higher_is_better": True,
+            "n_gpus": 1, "dtype": "bf16 x bf16 -> fp32", "data": "synthetic",
+            "config": {"workload": f"tensor-core GEMM M={m} N={N} K={kpad} (reprojection shape)"},
+            "peak": tpeak, "peak_source": tpeak_kind, **rows}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     args = parse_args()
+    if args.gemm:
+        return run_gemm(args)
     if args.learned:
         return run_learned(args)
     if args.workload == "large" and args.impl == "gb300" and not args.ess:

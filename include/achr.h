@@ -175,7 +175,7 @@ achr_status achr_get_directions(const achr_ctx *ctx, double *dirs_out);
 
 /* ---- Learned direction preconditioner (no reference counterpart) ----
  * A low-rank-plus-diagonal linear map L = [diag(exp(s)), U] (d x (d + r)) in
- * null-space coordinates, fitted to samples y = N^T (x - mu) of the plain
+ * the coordinates below, fitted to samples y = B^T (x - mu) of the plain
  * sampler by the Gaussian KL loss 1/2 tr(C^-1 Sigma) + 1/2 log det C with
  * C = L L^T = diag(exp(2 s)) + U U^T (minibatch Sigma, Adam), all on the GPU.
  * Its directions N L z, z ~ N(0, I), drive hit-and-run (achr_set_directions)
@@ -199,9 +199,21 @@ typedef struct achr_precond_stats {
 
 void achr_precond_default_options(achr_precond_options *opt);
 
-/* Y (d x P, row-major, leading dimension ldy, FP32) = N^T (x - mu) for the
- * chains of an n x P row-major block of points (mu: n doubles or NULL), as a
- * tensor-core GEMM with three BF16 split products.  Synchronises `stream`. */
+/* The preconditioner's coordinates.  Hit-and-run directions must stay in the
+ * polytope's affine hull, not just the null space of S: a reaction that has
+ * the same value in every warmup point (blocked, or pinned at a bound by the
+ * other constraints) must not move, or almost every random direction leaves
+ * the polytope at once.  The basis (n x d, column-major, orthonormal) spans
+ * {v : S v = 0, v_i = 0 for those reactions}; d and the number of pinned
+ * reactions come from achr_precond_dim, the basis from achr_get_precond_basis
+ * (host or device memory).  Built on first use. */
+achr_status achr_precond_dim(achr_ctx *ctx, int32_t *d_out, int32_t *n_frozen_out);
+achr_status achr_get_precond_basis(achr_ctx *ctx, double *basis_out);
+
+/* Y (d x P, row-major, leading dimension ldy, FP32) = B^T (x - mu), B the
+ * preconditioner's basis above, for the chains of an n x P row-major block of
+ * points (mu: n doubles or NULL), as a tensor-core GEMM with three BF16 split
+ * products.  Synchronises `stream`. */
 achr_status achr_null_coords(achr_ctx *ctx, int32_t n_points, const double *d_points, int64_t ld, const double *d_mu,
                              float *d_Y, int64_t ldy, void *stream);
 
@@ -216,7 +228,7 @@ achr_status achr_precond_train(int32_t d, int32_t r, int32_t n_samples, const fl
                                const achr_precond_options *opt, float *d_s, float *d_U, void *stream,
                                achr_precond_stats *stats);
 
-/* Pool of n_dirs directions N (exp(s) z1 + U z2), z ~ N(0, I) from Philox
+/* Pool of n_dirs directions B (exp(s) z1 + U z2), z ~ N(0, I) from Philox
  * keyed by seed, computed in FP64 (the directions lie in the null space of S
  * to rounding), installed with achr_set_directions. */
 achr_status achr_precond_pool(achr_ctx *ctx, int32_t r, const float *d_s, const float *d_U, int32_t n_dirs,

@@ -102,16 +102,33 @@ def test_training_fits_a_known_covariance(pkg):
     assert kl_fit < 0.05 * kl_init and kl_fit < kl_true + 0.2
 
 
+def test_precond_basis_spans_the_affine_hull(pkg, sampler, small_model, golden):
+    S = dense_S(small_model)
+    warm = golden["warmup"]
+    frozen = np.ptp(warm, axis=1) <= 1e-9 * np.maximum(1.0, np.abs(warm).max(axis=1))
+    d, nf = sampler.precond_dim()
+    B = sampler.precond_basis()
+    assert nf == int(frozen.sum()) and B.shape == (small_model.n_rxns, d)
+    assert np.abs(S @ B).max() <= 1e-12 and np.abs(B[frozen]).max() <= 1e-12
+    assert np.abs(B.T @ B - np.eye(d)).max() <= 1e-12
+    A = np.vstack([S, np.eye(S.shape[1])[frozen]])
+    lam, V = np.linalg.eigh(A.T @ A)
+    ref = V[:, lam < A.shape[1] * lam.max() * 2.2204e-16]
+    assert ref.shape[1] == d
+    assert np.abs(B @ B.T - ref @ ref.T).max() <= 1e-10  # same subspace
+
+
 def test_null_coords_match_numpy(pkg, sampler, golden):
     P = 300
     pts, _ = sampler.sample(P, 25, seed=9)
     mu = pts.mean(axis=1)
     X = _dev(pts, torch.float64)
     dmu = _dev(mu, torch.float64)
-    d = sampler.null_dim
+    Bas = sampler.precond_basis()
+    d = Bas.shape[1]
     Y = torch.full((d, P + 4), float("nan"), device="cuda")
     sampler.null_coords(P, X.data_ptr(), P, Y.data_ptr(), P + 4, d_mu=dmu.data_ptr())
-    ref = golden["N"].T @ (pts - mu[:, None])
+    ref = Bas.T @ (pts - mu[:, None])
     got = Y[:, :P].double().cpu().numpy()
     assert np.abs(got - ref).max() <= 1e-4 * np.abs(ref).max()
 
@@ -121,7 +138,8 @@ def test_learned_pool_directions_lie_in_null_space(pkg, small_model, golden):
     rng = np.random.default_rng(2)
     with pkg.Sampler(small_model, golden["warmup"]) as s:
         s.set_null_space(golden["N"])
-        d = s.null_dim
+        d, _ = s.precond_dim()
+        Bas = s.precond_basis()
         r = 4
         ds = _dev(0.1 * rng.standard_normal(d))
         dU = _dev(0.5 * rng.standard_normal((d, r)))
@@ -129,8 +147,8 @@ def test_learned_pool_directions_lie_in_null_space(pkg, small_model, golden):
         G = s.directions()
         assert G.shape == (s.n, 500)
         assert np.abs(S @ G).max() <= 1e-12 * np.abs(G).max()
-        # the pool's covariance in null-space coordinates approaches exp(2 s) + U U^T
-        Yc = golden["N"].T @ G
+        # the pool's covariance in the basis coordinates approaches exp(2 s) + U U^T
+        Yc = Bas.T @ G
         emp = Yc @ Yc.T / 500
         from oracle import precond
         C = precond.covariance(ds.cpu().numpy(), dU.cpu().numpy())
