@@ -64,12 +64,17 @@ __global__ void __launch_bounds__(256)
     const int i0 = blockIdx.y * kT, j0 = blockIdx.x * kT;
     float acc[4][4] = {};
     for (int k0 = 0; k0 < K; k0 += kTK) {
+        // Each operand's tile is loaded with consecutive threads on its
+        // contiguous index (k when the stride along k is 1, else the row index).
         for (int t = threadIdx.x; t < kT * kTK; t += 256) {
-            const int ii = t % kT, kk = t / kT;
+            const int ii = (sak == 1) ? t / kTK : t % kT, kk = (sak == 1) ? t % kTK : t / kT;
             const int i = i0 + ii, k = k0 + kk;
             As[kk][ii] = (i < M && k < K) ? A[(long long)i * sai + (long long)k * sak] : 0.0f;
-            const int j = j0 + ii;
-            Bs[kk][ii] = (j < N && k < K) ? B[(long long)k * sbk + (long long)j * sbj] : 0.0f;
+        }
+        for (int t = threadIdx.x; t < kT * kTK; t += 256) {
+            const int jj = (sbk == 1) ? t / kTK : t % kT, kk = (sbk == 1) ? t % kTK : t / kT;
+            const int j = j0 + jj, k = k0 + kk;
+            Bs[kk][jj] = (j < N && k < K) ? B[(long long)k * sbk + (long long)j * sbj] : 0.0f;
         }
         __syncthreads();
 #pragma unroll
@@ -239,6 +244,62 @@ __global__ void adam_kernel(long long n, float *__restrict__ p, const float *__r
     m[t] = mi;
     v[t] = vi;
     p[t] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+}
+
+// Root mean square of every row of Y (d x ns, leading dimension ldy): the
+// per-coordinate scale of centred samples.  One warp per row.
+__global__ void row_rms_kernel(int d, int ns, const float *__restrict__ Y, long long ldy, float *__restrict__ sig) {
+    const int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    if (i >= d) return;
+    double acc = 0.0;
+    for (int b = lane; b < ns; b += 32) {
+        const double y = Y[(long long)i * ldy + b];
+        acc += y * y;
+    }
+    for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) sig[i] = (float)fmax(sqrt(acc / (double)ns), 1e-30);
+}
+
+// Ys = Y / sig (rows), into a dense d x ns buffer.
+__global__ void scale_rows_kernel(int d, int ns, const float *__restrict__ Y, long long ldy,
+                                  const float *__restrict__ sig, float *__restrict__ Ys) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)d * ns) return;
+    const int i = (int)(t / ns), b = (int)(t % ns);
+    Ys[t] = Y[(long long)i * ldy + b] / sig[i];
+}
+
+// Parameters between original and standardised coordinates (y = sig * ys):
+// forward s -= log sig, U /= sig; backward s += log sig, U *= sig.
+__global__ void rescale_params_kernel(int d, int r, const float *__restrict__ sig, float *__restrict__ s,
+                                      float *__restrict__ U, int forward) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < (long long)d * r) {
+        const int i = (int)(t / r);
+        U[t] = forward ? U[t] / sig[i] : U[t] * sig[i];
+    }
+    if (t < d) s[t] += forward ? -logf(sig[t]) : logf(sig[t]);
+}
+
+__global__ void f32_to_f64_scaled_kernel(long long n, const float *__restrict__ in, double scale,
+                                         double *__restrict__ out) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) out[t] = scale * (double)in[t];
+}
+
+// Probabilistic-PCA start (the maximum-likelihood C = sigma^2 I + U U^T):
+// with eigenpairs (lam ascending, V column-major) of the sample covariance,
+// U = V_top (lam_top - sigma^2)^1/2, sigma^2 = mean of the other eigenvalues.
+__global__ void ppca_init_kernel(int d, int r, const double *__restrict__ V, const double *__restrict__ lam,
+                                 double sigma2, float *__restrict__ s, float *__restrict__ U) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < (long long)d * r) {
+        const int i = (int)(t / r), j = (int)(t % r);
+        const int col = d - r + j;
+        U[t] = (float)(V[(long long)col * d + i] * sqrt(fmax(lam[col] - sigma2, 0.0)));
+    }
+    if (t < d) s[t] = (float)(0.5 * log(sigma2));
 }
 
 // Standard normal (Box-Muller on two 32-bit Philox words) for entry (row, col).
@@ -470,6 +531,8 @@ void achr_precond_default_options(achr_precond_options *opt) {
     opt->beta2 = 0.999f;
     opt->eps = 1e-8f;
     opt->seed = 1;
+    opt->init = 1;
+    opt->standardize = 1;
 }
 
 achr_status achr_precond_loss_grad(int32_t d, int32_t r, int32_t B, const float *d_s, const float *d_U,
@@ -499,8 +562,70 @@ achr_status achr_precond_train(int32_t d, int32_t r, int32_t n_samples, const fl
     if (!opt || d <= 0 || r <= 0 || r > 1024 || !d_Y || !d_s || !d_U || n_samples <= 0 || ldy < n_samples ||
         opt->batch <= 0 || opt->batch > n_samples || opt->iterations < 0)
         return pc_err(ACHR_ERR_INVALID, "bad preconditioner training arguments");
+    if (opt->init && r >= d) return pc_err(ACHR_ERR_INVALID, "the PCA start needs rank < d");
     cudaStream_t st = (cudaStream_t)stream;
     const int B = opt->batch;
+    // Standardised coordinates: every coordinate scaled to unit RMS, so one
+    // learning rate suits coordinates whose spreads differ by orders of magnitude.
+    DevBuf<float> sig, Ys;
+    const float *Yt = d_Y;
+    long long ldt = ldy;
+    if (opt->standardize || opt->init) {
+        PC_TRY(sig.alloc(d));
+        row_rms_kernel<<<blocks_for(d, 8), 256, 0, st>>>(d, n_samples, d_Y, ldy, sig.p);
+        PC_TRY(cudaGetLastError());
+        if (opt->standardize) {
+            PC_TRY(Ys.alloc((size_t)d * n_samples));
+            scale_rows_kernel<<<blocks_for((long long)d * n_samples), 256, 0, st>>>(d, n_samples, d_Y, ldy, sig.p,
+                                                                                  Ys.p);
+            PC_TRY(cudaGetLastError());
+            Yt = Ys.p;
+            ldt = n_samples;
+        }
+    }
+    if (opt->init) {
+        // sample covariance of the (standardised) samples, its eigenpairs in FP64
+        DevBuf<float> Sig;
+        DevBuf<double> Sd, lam, work;
+        DevBuf<int> info;
+        PC_TRY(Sig.alloc((size_t)d * d));
+        PC_TRY(sgemm(st, d, d, n_samples, 1.0f, Yt, ldt, 1, Yt, 1, ldt, 0.0f, Sig.p, d));
+        PC_TRY(Sd.alloc((size_t)d * d));
+        f32_to_f64_scaled_kernel<<<blocks_for((long long)d * d), 256, 0, st>>>((long long)d * d, Sig.p,
+                                                                              1.0 / (double)n_samples, Sd.p);
+        PC_TRY(cudaGetLastError());
+        PC_TRY(lam.alloc(d));
+        PC_TRY(info.alloc(1));
+        cusolverDnHandle_t sh = nullptr;
+        if (cusolverDnCreate(&sh) != CUSOLVER_STATUS_SUCCESS) return pc_err(ACHR_ERR_CUDA, "cusolverDnCreate failed");
+        cusolverDnSetStream(sh, st);
+        int lwork = 0;
+        cusolverStatus_t ss =
+            cusolverDnDsyevd_bufferSize(sh, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, d, Sd.p, d, lam.p, &lwork);
+        if (ss == CUSOLVER_STATUS_SUCCESS) {
+            if (cudaError_t e = work.alloc((size_t)std::max(lwork, 1))) {
+                cusolverDnDestroy(sh);
+                return pc_err(ACHR_ERR_CUDA, std::string("syevd workspace: ") + cudaGetErrorString(e));
+            }
+            ss = cusolverDnDsyevd(sh, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, d, Sd.p, d, lam.p, work.p,
+                                  lwork, info.p);
+        }
+        cusolverDnDestroy(sh);
+        if (ss != CUSOLVER_STATUS_SUCCESS) return pc_err(ACHR_ERR_NUMERIC, "syevd of the sample covariance failed");
+        std::vector<double> hl((size_t)d);
+        PC_TRY(cudaMemcpyAsync(hl.data(), lam.p, sizeof(double) * d, cudaMemcpyDeviceToHost, st));
+        PC_TRY(cudaStreamSynchronize(st));
+        double sigma2 = 0.0;
+        for (int k = 0; k < d - r; ++k) sigma2 += std::max(hl[(size_t)k], 0.0);
+        sigma2 = std::max(sigma2 / (double)(d - r), 1e-12 * std::max(hl.back(), 1e-300));
+        ppca_init_kernel<<<blocks_for((long long)d * r), 256, 0, st>>>(d, r, Sd.p, lam.p, sigma2, d_s, d_U);
+        PC_TRY(cudaGetLastError());
+        if (!opt->standardize)  // the start is in standardised units: bring it back
+            rescale_params_kernel<<<blocks_for((long long)d * r), 256, 0, st>>>(d, r, sig.p, d_s, d_U, 0);
+    } else if (opt->standardize) {
+        rescale_params_kernel<<<blocks_for((long long)d * r), 256, 0, st>>>(d, r, sig.p, d_s, d_U, 1);
+    }
+    PC_TRY(cudaGetLastError());
     PcWork w;
     PC_TRY(w.alloc(d, r, B));
     DevBuf<float> gs, gU, ms, vs, mU, vU, losses;
@@ -539,8 +664,8 @@ achr_status achr_precond_train(int32_t d, int32_t r, int32_t n_samples, const fl
                 std::swap(order[(size_t)k], order[(size_t)((rs >> 33) % (uint64_t)(k + 1))]);
             }
         }
-        const float *Yb = d_Y + (size_t)order[(size_t)q] * B;
-        PC_TRY(loss_grad(st, d, r, B, d_s, d_U, Yb, ldy, w, gs.p, gU.p));
+        const float *Yb = Yt + (size_t)order[(size_t)q] * B;
+        PC_TRY(loss_grad(st, d, r, B, d_s, d_U, Yb, ldt, w, gs.p, gU.p));
         PC_TRY(cudaMemcpyAsync(losses.p + it, w.scal.p + 1, sizeof(float), cudaMemcpyDeviceToDevice, st));
         const float c1 = 1.0f - std::pow(opt->beta1, (float)(it + 1));
         const float c2 = 1.0f - std::pow(opt->beta2, (float)(it + 1));
@@ -549,6 +674,10 @@ achr_status achr_precond_train(int32_t d, int32_t r, int32_t n_samples, const fl
         adam_kernel<<<blocks_for((long long)d * r), 256, 0, st>>>((long long)d * r, d_U, gU.p, mU.p, vU.p,
                                                                   opt->learning_rate, opt->beta1, opt->beta2,
                                                                   opt->eps, c1, c2);
+        PC_TRY(cudaGetLastError());
+    }
+    if (opt->standardize) {  // parameters back to the caller's coordinates
+        rescale_params_kernel<<<blocks_for((long long)d * r), 256, 0, st>>>(d, r, sig.p, d_s, d_U, 0);
         PC_TRY(cudaGetLastError());
     }
     PC_TRY(cudaEventRecord(e1, st));

@@ -612,11 +612,9 @@ def run_learned(args):
                           stream=stream)
     del x, a
     Y -= Y.mean(dim=1, keepdim=True)
-    var = Y.var(dim=1).clamp_min(1e-30)
-    s_par = (0.5 * torch.log(var)).float().contiguous()
-    g = torch.Generator(device="cuda").manual_seed(args.seed)
-    U_par = (0.01 * torch.randn((d, args.precond_rank), device="cuda", generator=g) *
-             torch.exp(s_par)[:, None]).contiguous()
+    # start: the probabilistic-PCA fit of the samples (computed by the library)
+    s_par = torch.zeros(d, dtype=torch.float32, device="cuda")
+    U_par = torch.zeros((d, args.precond_rank), dtype=torch.float32, device="cuda")
     tst = pkg.precond_train(d, args.precond_rank, Pt * Ks, Y.data_ptr(), Pt * Ks, s_par.data_ptr(), U_par.data_ptr(),
                             stream=stream, iterations=args.iters, batch=args.batch, learning_rate=args.lr,
                             seed=args.seed)

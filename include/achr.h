@@ -188,6 +188,9 @@ typedef struct achr_precond_options {
     float beta1, beta2;    /* 0.9, 0.999 */
     float eps;             /* 1e-8 */
     uint64_t seed;         /* order in which minibatches are visited */
+    int32_t init;          /* 1: start from the probabilistic-PCA fit of the samples (overwrites s, U);
+                              0: start from the s, U passed in */
+    int32_t standardize;   /* 1: train in coordinates scaled to unit RMS (results returned unscaled) */
 } achr_precond_options;
 
 typedef struct achr_precond_stats {
@@ -222,8 +225,10 @@ achr_status achr_precond_loss_grad(int32_t d, int32_t r, int32_t B, const float 
                                    const float *d_Y, int64_t ldy, float *loss_out, float *d_gs, float *d_gU,
                                    void *stream);
 
-/* opt.iterations Adam steps from the given s, U (updated in place) over
- * minibatches of consecutive columns of Y.  Synchronises `stream`. */
+/* opt.iterations Adam steps over minibatches of consecutive columns of Y
+ * (centred samples), from the probabilistic-PCA fit of Y (opt.init = 1) or
+ * from the s, U passed in; s and U are updated in place.  Synchronises
+ * `stream`. */
 achr_status achr_precond_train(int32_t d, int32_t r, int32_t n_samples, const float *d_Y, int64_t ldy,
                                const achr_precond_options *opt, float *d_s, float *d_U, void *stream,
                                achr_precond_stats *stats);

@@ -32,6 +32,7 @@ def test_philox_matches_curand(curand_lib, oracle_mod):
     rng = np.random.default_rng(2026)
     n = 4096
     ctr = rng.integers(0, 2 ** 32, size=(n, 4), dtype=np.uint64)
+    ctr[:, 1] >>= np.uint64(2)  # the offset argument is 4 x (c1:c0) in 64 bits: c1 < 2^30
     key = rng.integers(0, 2 ** 32, size=(n, 2), dtype=np.uint64)
     ctr[:8] = 0  # include the all-zero counter and small counters
     ctr[8:16, 0] = np.arange(8)

@@ -118,6 +118,33 @@ def test_precond_basis_spans_the_affine_hull(pkg, sampler, small_model, golden):
     assert np.abs(B @ B.T - ref @ ref.T).max() <= 1e-10  # same subspace
 
 
+def test_training_start_options(pkg):
+    """Zero steps: a given start comes back unchanged through the standardisation; the
+    probabilistic-PCA start is the maximum-likelihood sigma^2 I + U U^T of the samples."""
+    from oracle import precond
+    rng = np.random.default_rng(8)
+    d, r, n = 40, 3, 8192
+    Y = (rng.standard_normal((d, r)) @ rng.standard_normal((r, n)) * 3.0 + 0.5 * rng.standard_normal((d, n)))
+    Y *= np.exp(rng.uniform(-2, 2, (d, 1)))
+    s0 = 0.2 * rng.standard_normal(d)
+    U0 = rng.standard_normal((d, r))
+    ds, dU, dY = _dev(s0), _dev(U0), _dev(Y)
+    pkg.precond_train(d, r, n, dY.data_ptr(), n, ds.data_ptr(), dU.data_ptr(), iterations=0, batch=256, init=0,
+                      standardize=1)
+    assert np.allclose(ds.cpu().numpy(), s0, atol=1e-5) and np.allclose(dU.cpu().numpy(), U0, rtol=1e-5, atol=1e-5)
+    pkg.precond_train(d, r, n, dY.data_ptr(), n, ds.data_ptr(), dU.data_ptr(), iterations=0, batch=256, init=1,
+                      standardize=1)
+    s_p, U_p = ds.cpu().numpy().astype(np.float64), dU.cpu().numpy().astype(np.float64)
+    # reference PPCA in standardised coordinates, mapped back
+    sig = np.sqrt((Y ** 2).mean(axis=1))
+    Z = Y / sig[:, None]
+    lam, V = np.linalg.eigh(Z @ Z.T / n)
+    s2 = lam[: d - r].mean()
+    C_ref = np.diag(sig) @ (s2 * np.eye(d) + (V[:, d - r:] * (lam[d - r:] - s2)) @ V[:, d - r:].T) @ np.diag(sig)
+    C_got = precond.covariance(s_p, U_p)
+    assert np.abs(C_got - C_ref).max() <= 1e-3 * np.abs(C_ref).max()
+
+
 def test_null_coords_match_numpy(pkg, sampler, golden):
     P = 300
     pts, _ = sampler.sample(P, 25, seed=9)
