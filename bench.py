@@ -68,6 +68,8 @@ def parse_args():
     ap.add_argument("--batch", type=int, default=4096)
     ap.add_argument("--lr", type=float, default=0.01)
     ap.add_argument("--pool", type=int, default=16384)
+    ap.add_argument("--refine", type=int, default=0,
+                    help="re-fit the preconditioner this many times on the learned sampler's own samples")
     ap.add_argument("--large-chains", type=int, default=262_144, help="chains of the large workload")
     ap.add_argument("--large-steps", type=int, default=200, help="timed steps of the large workload")
     ap.add_argument("--profile-case", type=int, nargs=2, metavar=("CHAINS", "STEPS"),
@@ -570,6 +572,8 @@ def run_learned(args):
     3. A pool of --pool directions B L z (B: the basis of the directions the
        polytope spans) is installed (achr_precond_pool); the sampler then runs
        hit-and-run.
+       With --refine R the fit is repeated R times on samples of the learned
+       sampler itself (same schedule, fresh chain ids).
     4. Both samplers run the same ESS schedule (--learned CHAINS BURNIN SEGMENTS
        STEPS, fresh chains from the warmup centre, another seed); min-ESS/s
        counts the device time of the sampling launches.  If the learned
@@ -618,6 +622,26 @@ def run_learned(args):
     tst = pkg.precond_train(d, args.precond_rank, Pt * Ks, Y.data_ptr(), Pt * Ks, s_par.data_ptr(), U_par.data_ptr(),
                             stream=stream, iterations=args.iters, batch=args.batch, learning_rate=args.lr,
                             seed=args.seed)
+    refine = []
+    for rnd in range(args.refine):
+        # re-fit on samples of the learned sampler itself (same schedule, fresh chain ids)
+        plain.precond_pool(args.precond_rank, s_par.data_ptr(), U_par.data_ptr(), args.pool, seed=args.seed + 11)
+        x = torch.zeros((n, Pt), dtype=torch.float64, device="cuda")
+        a = torch.zeros_like(x)
+        off = (rnd + 1) * Pt
+        st = plain.sample_resume(Pt, 0, Tb, False, x.data_ptr(), a.data_ptr(), Pt, stream=stream,
+                                 seed=args.seed + 7, chain_offset=off, with_stats=True)
+        for k in range(Ks):
+            plain.sample_resume(Pt, Tb + k * Lg, Lg, True, x.data_ptr(), a.data_ptr(), Pt, stream=stream,
+                                seed=args.seed + 7, chain_offset=off)
+            plain.null_coords(Pt, x.data_ptr(), Pt, Y.data_ptr() + 4 * k * Pt, Pt * Ks, d_mu=mu.data_ptr(),
+                              stream=stream)
+        del x, a
+        plain.set_directions(None)
+        Y -= Y.mean(dim=1, keepdim=True)
+        refine.append(pkg.precond_train(d, args.precond_rank, Pt * Ks, Y.data_ptr(), Pt * Ks, s_par.data_ptr(),
+                                        U_par.data_ptr(), stream=stream, iterations=args.iters, batch=args.batch,
+                                        learning_rate=args.lr, seed=args.seed + rnd + 1))
     del Y
     torch.cuda.empty_cache()
     train_s = time.perf_counter() - t_train
@@ -647,7 +671,7 @@ def run_learned(args):
         "learned_over_plain": ll["min_ess_per_s"] / lp["min_ess_per_s"], "fallback_to_plain": fallback,
         "plain": lp, "learned": ll,
         "training": {"samples": Pt * Ks, "basis_dim": d, "null_dim": null_dim, "pinned_reactions": n_frozen,
-                     "generation_ms": gen_ms, **tst, "total_s": train_s},
+                     "generation_ms": gen_ms, **tst, "refine_rounds": refine, "total_s": train_s},
         "setup_s": setup_s,
     }
     print(json.dumps(line), flush=True)
