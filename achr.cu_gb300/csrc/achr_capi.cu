@@ -126,8 +126,9 @@ achr_status validate_options(const achr_options &o) {
     if (o.max_attempts <= 0) return fail(ACHR_ERR_INVALID, "max_attempts must be positive");
     if (o.centre_offset != 0 && o.centre_offset != 1) return fail(ACHR_ERR_INVALID, "centre_offset must be 0 or 1");
     if (o.threads_per_chain != 0 && o.threads_per_chain != 32 && o.threads_per_chain != 64 &&
-        o.threads_per_chain != 128 && o.threads_per_chain != 256 && o.threads_per_chain != 512)
-        return fail(ACHR_ERR_INVALID, "threads_per_chain must be 0, 32, 64, 128, 256 or 512");
+        o.threads_per_chain != 128 && o.threads_per_chain != 256 && o.threads_per_chain != 320 &&
+        o.threads_per_chain != 384 && o.threads_per_chain != 512)
+        return fail(ACHR_ERR_INVALID, "threads_per_chain must be 0, 32, 64, 128, 256, 320, 384 or 512");
     if (!(o.residual_tol >= 0) || !(o.max_min_tol >= 0) || !(o.u_tol >= 0) || !(o.d_tol >= 0) ||
         !(o.feasibility_tol >= 0))
         return fail(ACHR_ERR_INVALID, "tolerances must be non-negative");

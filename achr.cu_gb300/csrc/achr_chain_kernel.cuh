@@ -266,7 +266,7 @@ inline size_t chain_smem_bytes_cfg(int np, int d, int bd) {
 }
 
 template <int BD, int EPT>
-__global__ void __launch_bounds__(BD, (BD <= 256 ? 2 : 1)) achr_chain_kernel(const ChainArgs a) {
+__global__ void __launch_bounds__(BD, (BD <= 384 ? 2 : 1)) achr_chain_kernel(const ChainArgs a) {
     constexpr int NP = BD * EPT;
     constexpr int NW = BD / 32;
     extern __shared__ __align__(128) unsigned char smem_raw[];

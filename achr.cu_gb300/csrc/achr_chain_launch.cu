@@ -10,6 +10,7 @@ namespace achr {
 
 cudaError_t launch_chain_cfg_small(int bd, int ept, const ChainArgs &a, cudaStream_t s, int max_ctas, int *per_sm);
 cudaError_t launch_chain_cfg_large(int bd, int ept, const ChainArgs &a, cudaStream_t s, int max_ctas, int *per_sm);
+cudaError_t launch_chain_cfg_mid(int bd, int ept, const ChainArgs &a, cudaStream_t s, int max_ctas, int *per_sm);
 
 namespace {
 
@@ -19,10 +20,15 @@ struct Cfg {
 };
 
 // Ordered by padded length; the default for each length comes first.
+// 320 x 12 and 384 x 10 (3840 elements) put 20 or 24 warps on an SM with two
+// chains each, against 16 for 256 x 16, at the cost of fewer registers per
+// thread; 384 x 10 is the default up to 3840 reactions (2.04e7 against 1.95e7
+// chain-steps/s for 256 x 16 on a 2766 x 3742 model).
 const Cfg kLadder[] = {
-    {32, 4, true},   {64, 4, true},   {32, 8, false},  {128, 4, true},  {64, 8, false},
-    {128, 8, true},  {256, 4, false}, {256, 8, true},  {128, 16, false}, {512, 4, false},
-    {256, 16, true}, {512, 8, false}, {128, 32, false}, {512, 16, true}, {512, 32, true},
+    {32, 4, true},    {64, 4, true},    {32, 8, false},   {128, 4, true},  {64, 8, false},
+    {128, 8, true},   {256, 4, false},  {256, 8, true},   {128, 16, false}, {512, 4, false},
+    {320, 12, false}, {384, 10, true},  {256, 16, true},  {512, 8, false},  {128, 32, false},
+    {512, 16, true},  {512, 32, true},
 };
 
 const Cfg *find_cfg(int n, int threads_per_chain) {
@@ -56,7 +62,7 @@ int chain_candidates(int n, int max_np, int *bds, int cap) {
     int k = 0;
     for (const Cfg &c : kLadder) {
         const int np = c.bd * c.ept;
-        if (np < n || np > max_np || (np != np0 && np != 2 * np0)) continue;
+        if (np < n || np > max_np || np > 2 * np0) continue;
         bool dup = false;
         for (int j = 0; j < k; ++j) dup |= bds[j] == c.bd;
         if (dup || chain_padded_length(n, c.bd) != np) continue;
@@ -77,8 +83,9 @@ cudaError_t launch_chains(const ChainArgs &a, int threads_per_chain, cudaStream_
     const Cfg *c = find_cfg(a.n, threads_per_chain);
     if (!c || c->bd * c->ept > a.np) return cudaErrorInvalidValue;
     if (a.P <= 0 && !per_sm) return cudaSuccess;
-    return c->bd <= 128 ? launch_chain_cfg_small(c->bd, c->ept, a, stream, max_ctas, per_sm)
-                        : launch_chain_cfg_large(c->bd, c->ept, a, stream, max_ctas, per_sm);
+    if (c->bd <= 128) return launch_chain_cfg_small(c->bd, c->ept, a, stream, max_ctas, per_sm);
+    if (c->bd == 320 || c->bd == 384) return launch_chain_cfg_mid(c->bd, c->ept, a, stream, max_ctas, per_sm);
+    return launch_chain_cfg_large(c->bd, c->ept, a, stream, max_ctas, per_sm);
 }
 
 }  // namespace achr

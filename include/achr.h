@@ -72,7 +72,8 @@ typedef struct {
     int32_t max_attempts;     /* rejected redraws of one step before a chain stops (default 100000) */
     int32_t centre_offset;    /* 0: centre weights of ACHRCuda.cu:347-348; 1: ACHRSamplerMOD.m:174 */
     int32_t exact_ratio;      /* 1: evaluate every ratio-test candidate in FP64 (diagnostic, slower) */
-    int32_t threads_per_chain;/* 0: chosen by size; else 32, 64, 128, 256 or 512 threads per chain */
+    int32_t threads_per_chain;/* 0: chosen by size; else 32, 64, 128, 256, 320, 384 or 512 threads per chain
+                                 (320 and 384 hold up to 3840 reactions) */
     int32_t reserved;
     double residual_tol;      /* 1e-9 (ACHRCuda.cu:338) */
     double max_min_tol;       /* 1e-9 (ACHRCuda.cu:505) */
