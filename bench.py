@@ -68,6 +68,8 @@ def parse_args():
     ap.add_argument("--batch", type=int, default=4096)
     ap.add_argument("--lr", type=float, default=0.01)
     ap.add_argument("--pool", type=int, default=16384)
+    ap.add_argument("--start", choices=["warmup", "centre"], default="warmup",
+                    help="ESS runs: chains start at random warmup points (over-dispersed, default) or at the centre")
     ap.add_argument("--refine", type=int, default=0,
                     help="re-fit the preconditioner this many times on the learned sampler's own samples")
     ap.add_argument("--large-chains", type=int, default=262_144, help="chains of the large workload")
@@ -497,8 +499,22 @@ def run_batch(args):
     return 0
 
 
-def ess_trace(smp, M, B, K, L, seed, stream):
-    """Chains from the warmup centre: B burn-in steps, then K segments of L steps
+def dispersed_starts(warm, M, seed):
+    """Over-dispersed starting points for R-hat: chain p starts at a random warmup point
+    (seeded), with the centre accumulator of a fresh chain, (W) * centre of the warmups."""
+    import torch
+
+    rng = np.random.default_rng(seed)
+    idx = torch.from_numpy(rng.integers(0, warm.shape[1], size=M))
+    w = torch.from_numpy(np.ascontiguousarray(warm)).cuda()
+    x0 = w[:, idx.cuda()].contiguous()
+    a0 = (float(warm.shape[1]) * w.mean(dim=1, keepdim=True)).expand(-1, M).contiguous()
+    return x0, a0
+
+
+def ess_trace(smp, M, B, K, L, seed, stream, starts=None):
+    """Chains from the warmup centre (starts None, the reference's start) or from given
+    (x0, A0) device states: B burn-in steps, then K segments of L steps
     (achr_sample_resume); the points after every segment are the draws.
     Returns (draws (chains, draws, fluxes), device ms of all launches, chain-steps)."""
     import torch
@@ -507,8 +523,11 @@ def ess_trace(smp, M, B, K, L, seed, stream):
     pts = torch.zeros((n, M), dtype=torch.float64, device="cuda")
     acc = torch.zeros((n, M), dtype=torch.float64, device="cuda")
     trace = torch.empty((K, n, M), dtype=torch.float64, device="cuda")
-    st = smp.sample_resume(M, 0, B, False, pts.data_ptr(), acc.data_ptr(), M, stream=stream, seed=seed,
-                           with_stats=True)
+    if starts is not None:
+        pts.copy_(starts[0])
+        acc.copy_(starts[1])
+    st = smp.sample_resume(M, 0, B, starts is not None, pts.data_ptr(), acc.data_ptr(), M, stream=stream,
+                           seed=seed, with_stats=True)
     ms, steps = st["kernel_ms"], st["accepted"]
     for k in range(K):
         st = smp.sample_resume(M, B + k * L, L, True, pts.data_ptr(), acc.data_ptr(), M, stream=stream, seed=seed,
@@ -541,7 +560,8 @@ def run_ess(args):
     n = spec.n_rxns
     smp = pkg.Sampler(model, warm)
     stream = torch.cuda.current_stream().cuda_stream
-    draws, ms, acc_steps = ess_trace(smp, M, B, K, L, args.seed, stream)
+    starts = dispersed_starts(warm, M, args.seed + 5) if args.start == "warmup" else None
+    draws, ms, acc_steps = ess_trace(smp, M, B, K, L, args.seed, stream, starts=starts)
     t0 = time.perf_counter()
     summ = diag.summarize(draws)
     diag_s = time.perf_counter() - t0
@@ -549,7 +569,8 @@ def run_ess(args):
         "metric": "min-ESS/s", "value": summ["min_ess"] / (ms * 1e-3), "unit": "effective samples/s",
         "higher_is_better": True, "n_gpus": 1, "dtype": "f64", "data": "synthetic",
         "config": {"workload": f"{args.workload}: {spec.n_mets}x{n}, {M} chains, {B} burn-in steps, {K} draws "
-                               f"{L} steps apart, plain ACHR (reference semantics)"},
+                               f"{L} steps apart, plain ACHR (reference semantics), chains start at "
+                               f"{'random warmup points' if args.start == 'warmup' else 'the warmup centre'}"},
         "max_rhat": summ["max_rhat"], "rhat_below_1.01": summ["max_rhat"] < 1.01, "min_ess": summ["min_ess"],
         "median_rhat": summ["median_rhat"], "rhat_q99": summ["rhat_q99"], "median_ess": summ["median_ess"],
         "fluxes": summ["params"], "frozen_fluxes": summ["frozen_params"], "sampling_ms": ms,
@@ -649,11 +670,12 @@ def run_learned(args):
     # 4. ESS comparison on the same schedule; the same context switches to the
     # learned pool after the plain run, so both use the same basis.
     M, B, K, L = args.learned
+    starts = dispersed_starts(warm, M, args.seed + 5) if args.start == "warmup" else None
     out = {}
     for name in ("plain", "learned"):
         if name == "learned":
             plain.precond_pool(args.precond_rank, s_par.data_ptr(), U_par.data_ptr(), args.pool, seed=args.seed + 11)
-        draws, ms, steps = ess_trace(plain, M, B, K, L, args.seed + 101, stream)
+        draws, ms, steps = ess_trace(plain, M, B, K, L, args.seed + 101, stream, starts=starts)
         summ = diag.summarize(draws)
         out[name] = {"min_ess_per_s": summ["min_ess"] / (ms * 1e-3), "min_ess": summ["min_ess"],
                      "max_rhat": summ["max_rhat"], "median_rhat": summ["median_rhat"],
@@ -665,7 +687,9 @@ def run_learned(args):
         "metric": "min-ESS/s", "value": lp["min_ess_per_s"] if fallback else ll["min_ess_per_s"],
         "unit": "effective samples/s", "higher_is_better": True, "n_gpus": 1, "dtype": "f64", "data": "synthetic",
         "config": {"workload": f"{args.workload}: {spec.n_mets}x{n}, {M} chains, {B} burn-in steps, {K} draws {L} "
-                               f"steps apart; learned: rank {args.precond_rank} + diagonal, {args.iters} Adam steps on "
+                               f"steps apart, chains start at "
+                               f"{'random warmup points' if args.start == 'warmup' else 'the warmup centre'}; "
+                               f"learned: rank {args.precond_rank} + diagonal, {args.iters} Adam steps on "
                                f"{Pt * Ks} plain-ACHR samples, pool of {args.pool} directions",
                    "threads_per_chain": tpc},
         "learned_over_plain": ll["min_ess_per_s"] / lp["min_ess_per_s"], "fallback_to_plain": fallback,
