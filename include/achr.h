@@ -5,6 +5,8 @@
  * Plain pointers and sizes only; every call returns an achr_status and never
  * throws or exits.  achr_last_error() gives a message for the calling thread.
  * One context owns device copies of one model and its warmup points on one GPU.
+ * A context is used by one host thread at a time (its counters and scratch
+ * buffers are shared by its calls); distinct contexts may be used concurrently.
  *
  * Each entry point names the part of the reference program it replaces
  * (ACHRcu/ACHRCuda.cu in marouenbg/ACHR.cu).  The reference exposes a CLI,
