@@ -425,6 +425,29 @@ achr_status achr_create(const achr_model *model, const double *warmup, int32_t n
         ACHR_CUDA_TRY(ctx->rowptr.upload(rp.data(), rp.size()));
         ACHR_CUDA_TRY(ctx->colidx.upload(ci.data(), ci.size()));
         ACHR_CUDA_TRY(ctx->val.upload(vv.data(), vv.size()));
+        // Sliced ELL: groups of 32 consecutive (sorted) rows, each group padded
+        // to its longest row with (column 0, value 0) and stored slot-major,
+        // so a warp's 32 lanes read one nonzero slot as one coalesced segment.
+        const int groups = (m + 31) / 32;
+        std::vector<int> so((size_t)groups + 1, 0), sc;
+        std::vector<double> sv;
+        for (int g = 0; g < groups; ++g) {
+            int len = 0;
+            for (int l = 0; l < 32 && 32 * g + l < m; ++l)
+                len = std::max(len, rp[(size_t)(32 * g + l) + 1] - rp[(size_t)(32 * g + l)]);
+            so[(size_t)g + 1] = so[(size_t)g] + 32 * len;
+            for (int t = 0; t < len; ++t)
+                for (int l = 0; l < 32; ++l) {
+                    const int row = 32 * g + l;
+                    const bool real = row < m && t < rp[(size_t)row + 1] - rp[(size_t)row];
+                    sc.push_back(real ? ci[(size_t)rp[(size_t)row] + t] : 0);
+                    sv.push_back(real ? vv[(size_t)rp[(size_t)row] + t] : 0.0);
+                }
+        }
+        ctx->sell_groups = groups;
+        ACHR_CUDA_TRY(ctx->sell_off.upload(so.data(), so.size()));
+        ACHR_CUDA_TRY(ctx->sell_col.upload(sc.data(), sc.size()));
+        ACHR_CUDA_TRY(ctx->sell_val.upload(sv.data(), sv.size()));
     }
     ACHR_CUDA_TRY(ctx->counters.alloc(achr::CNT_SLOTS));
 
@@ -554,6 +577,10 @@ ChainArgs chain_args(const achr_ctx *ctx, uint64_t seed, uint64_t chain_offset, 
     a.row_ptr = ctx->rowptr.p;
     a.col_idx = ctx->colidx.p;
     a.val = ctx->val.p;
+    a.sell_off = ctx->sell_groups > 0 ? ctx->sell_off.p : nullptr;
+    a.sell_col = ctx->sell_col.p;
+    a.sell_val = ctx->sell_val.p;
+    a.sell_groups = ctx->sell_groups;
     a.N = ctx->N.p;
     a.out = d_points_out;
     a.ld_out = ld_out;

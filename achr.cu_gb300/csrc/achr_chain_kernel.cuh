@@ -253,6 +253,39 @@ __device__ __forceinline__ void bracket(double x, double dk, float2 b, float ber
     fl |= (!ok && !bad && !u_ok && !u_bad) ? 4 : 0;  // needs the FP64 norm
 }
 
+// Largest |(S x)_i| over this thread's rows, as the bits of a non-negative
+// double (reference findMaxAbs, ACHRCuda.cu:232-240, on the rows thread tid
+// owns: tid, tid + BD, ...; a warp's 32 lanes own 32 consecutive rows).  With
+// the sliced-ELL copy of S each warp's loads of one nonzero slot are one
+// coalesced segment; without it (caller-owned models) the CSR rows are read
+// directly.  Both visit a row's nonzeros in the same order, so the sums are
+// bitwise equal (the ELL padding adds 0 * x_0).
+template <int BD>
+__device__ __forceinline__ unsigned long long residual_max_bits(const ChainArgs &a, const double *xs, int tid) {
+    unsigned long long mx = 0;
+    if (a.sell_off) {
+        const int lane = tid & 31;
+        for (int g = tid >> 5; g < a.sell_groups; g += BD / 32) {
+            const int base = __ldg(a.sell_off + g);
+            const int len = (__ldg(a.sell_off + g + 1) - base) >> 5;
+            double acc = 0.0;
+            for (int t = 0; t < len; ++t) {
+                const int q = base + (t << 5) + lane;
+                acc = fma(__ldg(a.sell_val + q), xs[__ldg(a.sell_col + q)], acc);
+            }
+            mx = umax(mx, abs_bits(acc));
+        }
+    } else {
+        for (int row = tid; row < a.m; row += BD) {
+            double acc = 0.0;
+            const int q1 = __ldg(a.row_ptr + row + 1);
+            for (int q = __ldg(a.row_ptr + row); q < q1; ++q) acc = fma(__ldg(a.val + q), xs[__ldg(a.col_idx + q)], acc);
+            mx = umax(mx, abs_bits(acc));
+        }
+    }
+    return mx;
+}
+
 }  // namespace
 
 constexpr int kTbl = 64;  // steps per refill of the step table
@@ -668,14 +701,7 @@ __global__ void __launch_bounds__(BD, (BD <= 384 ? 2 : 1)) achr_chain_kernel(con
                     }
                     __syncthreads();
                     if (tid == 0) ++cnt[CNT_CHECKS];
-                    unsigned long long mx = 0;
-                    for (int row = tid; row < a.m; row += BD) {
-                        double acc = 0.0;
-                        const int q1 = __ldg(a.row_ptr + row + 1);
-                        for (int q = __ldg(a.row_ptr + row); q < q1; ++q)
-                            acc = fma(__ldg(a.val + q), xs[__ldg(a.col_idx + q)], acc);
-                        mx = umax(mx, abs_bits(acc));
-                    }
+                    unsigned long long mx = residual_max_bits<BD>(a, xs, tid);
 #pragma unroll
                     for (int o = 16; o; o >>= 1) mx = umax(mx, shfl_u64(mx, o));
                     if (lane == 0) rs->max4[warp] = mx;
@@ -760,14 +786,7 @@ __global__ void __launch_bounds__(BD, (BD <= 384 ? 2 : 1)) achr_chain_kernel(con
             const int n = a.n;
             unsigned long long res = 0;
             for (int pass = 0; pass < 2; ++pass) {
-                unsigned long long mx = 0;
-                for (int row = tid; row < a.m; row += BD) {
-                    double acc = 0.0;
-                    const int q1 = __ldg(a.row_ptr + row + 1);
-                    for (int q = __ldg(a.row_ptr + row); q < q1; ++q)
-                        acc = fma(__ldg(a.val + q), xs[__ldg(a.col_idx + q)], acc);
-                    mx = umax(mx, abs_bits(acc));
-                }
+                unsigned long long mx = residual_max_bits<BD>(a, xs, tid);
 #pragma unroll
                 for (int o = 16; o; o >>= 1) mx = umax(mx, shfl_u64(mx, o));
                 __syncthreads();

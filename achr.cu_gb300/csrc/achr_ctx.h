@@ -57,6 +57,9 @@ struct achr_ctx {
     achr::DevBuf<double2> lbub;
     achr::DevBuf<float2> bnd;
     achr::DevBuf<int> rowptr, colidx;  // device CSR: rows sorted longest first
+    achr::DevBuf<int> sell_off, sell_col;  // the same rows as sliced ELL (32-row groups)
+    achr::DevBuf<double> sell_val;
+    int sell_groups = 0;
     achr::DevBuf<unsigned long long> counters;
     achr::ReprojState *reproj = nullptr;  // batched reprojection operator, built on first use
     achr::DevBuf<double> dirs;   // hit-and-run direction pool, n x n_dirs (leading dimension ldw)

@@ -42,6 +42,12 @@ struct ChainArgs {
     const int *row_ptr;         // CSR of S (m + 1)
     const int *col_idx;
     const double *val;
+    // Sliced ELL copy of the same rows (groups of 32 rows, slot t of lane l of
+    // group g at sell_off[g] + 32 t + l, zero padding); sell_off NULL: use CSR.
+    const int *sell_off;
+    const int *sell_col;
+    const double *sell_val;
+    int sell_groups;
     const double *N;            // n x d column-major null-space basis (ld = n)
     double *out;                // n x P row-major block: out[i * ld_out + p]
     long long ld_out;
