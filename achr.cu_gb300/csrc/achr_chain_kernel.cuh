@@ -269,7 +269,8 @@ __device__ __forceinline__ unsigned long long residual_max_bits(const ChainArgs 
             const int base = __ldg(a.sell_off + g);
             const int len = (__ldg(a.sell_off + g + 1) - base) >> 5;
             double acc = 0.0;
-            for (int t = 0; t < len; ++t) {
+#pragma unroll 4
+            for (int t = 0; t < len; ++t) {  // unrolled so the loads of 4 slots are in flight together
                 const int q = base + (t << 5) + lane;
                 acc = fma(__ldg(a.sell_val + q), xs[__ldg(a.sell_col + q)], acc);
             }
