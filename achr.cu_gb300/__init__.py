@@ -62,7 +62,7 @@ class Options(C.Structure):
     _fields_ = [
         ("mode", C.c_int32), ("null_space", C.c_int32), ("check_period", C.c_int32), ("max_attempts", C.c_int32),
         ("centre_offset", C.c_int32), ("exact_ratio", C.c_int32), ("threads_per_chain", C.c_int32),
-        ("reserved", C.c_int32),
+        ("reproject_form", C.c_int32),
         ("residual_tol", C.c_double), ("max_min_tol", C.c_double), ("u_tol", C.c_double), ("d_tol", C.c_double),
         ("feasibility_tol", C.c_double),
     ]

@@ -124,6 +124,7 @@ achr_status validate_options(const achr_options &o) {
         return fail(ACHR_ERR_INVALID, "unknown null_space method");
     if (o.check_period < 0) return fail(ACHR_ERR_INVALID, "check_period must be >= 0 (0: no in-loop checks)");
     if (o.max_attempts <= 0) return fail(ACHR_ERR_INVALID, "max_attempts must be positive");
+    if (o.reproject_form < 0 || o.reproject_form > 2) return fail(ACHR_ERR_INVALID, "reproject_form must be 0, 1 or 2");
     if (o.centre_offset != 0 && o.centre_offset != 1) return fail(ACHR_ERR_INVALID, "centre_offset must be 0 or 1");
     if (o.threads_per_chain != 0 && o.threads_per_chain != 32 && o.threads_per_chain != 64 &&
         o.threads_per_chain != 128 && o.threads_per_chain != 256 && o.threads_per_chain != 320 &&
@@ -448,6 +449,24 @@ achr_status achr_create(const achr_model *model, const double *warmup, int32_t n
         ACHR_CUDA_TRY(ctx->sell_off.upload(so.data(), so.size()));
         ACHR_CUDA_TRY(ctx->sell_col.upload(sc.data(), sc.size()));
         ACHR_CUDA_TRY(ctx->sell_val.upload(sv.data(), sv.size()));
+        // CSC over the same (sorted) rows, for the transposed product S^T z.
+        ctx->h_row_order = order_r;
+        std::vector<int> cp((size_t)n + 1, 0), cr(ci.size());
+        std::vector<double> cv(ci.size());
+        for (int c : ci) cp[(size_t)c + 1]++;
+        for (int j = 0; j < n; ++j) cp[(size_t)j + 1] += cp[(size_t)j];
+        {
+            std::vector<int> fill(cp.begin(), cp.end() - 1);
+            for (int q = 0; q < m; ++q)
+                for (int t = rp[(size_t)q]; t < rp[(size_t)q + 1]; ++t) {
+                    const int dst = fill[(size_t)ci[(size_t)t]]++;
+                    cr[(size_t)dst] = q;
+                    cv[(size_t)dst] = vv[(size_t)t];
+                }
+        }
+        ACHR_CUDA_TRY(ctx->csc_ptr.upload(cp.data(), cp.size()));
+        ACHR_CUDA_TRY(ctx->csc_row.upload(cr.data(), cr.size()));
+        ACHR_CUDA_TRY(ctx->csc_val.upload(cv.data(), cv.size()));
     }
     ACHR_CUDA_TRY(ctx->counters.alloc(achr::CNT_SLOTS));
 
@@ -478,6 +497,14 @@ achr_status achr_create(const achr_model *model, const double *warmup, int32_t n
     }
     st = upload_null_space(ctx, Nh.data(), d);
     if (st != ACHR_OK) return st;
+    // Large models reproject a chain through (S S^T)^+ on the residual (about
+    // m^2 FP32 operations) instead of N (N^T x) (4 n d FP64 operations).
+    const bool want_residual_form =
+        opt.reproject_form == 2 || (opt.reproject_form == 0 && (double)n * (double)d >= 4.0e6);
+    if (want_residual_form && m > 0 && m <= std::min(np, 8192)) {
+        st = achr::build_pinv32(ctx);
+        if (st != ACHR_OK) return st;
+    }
 
     // Centre of the warmup points and the centre accumulator (after the
     // FEASIBLE-mode projection of the warmup points).
@@ -577,6 +604,10 @@ ChainArgs chain_args(const achr_ctx *ctx, uint64_t seed, uint64_t chain_offset, 
     a.row_ptr = ctx->rowptr.p;
     a.col_idx = ctx->colidx.p;
     a.val = ctx->val.p;
+    a.pinv32 = ctx->pinv32.p;
+    a.csc_ptr = ctx->csc_ptr.p;
+    a.csc_row = ctx->csc_row.p;
+    a.csc_val = ctx->csc_val.p;
     a.sell_off = ctx->sell_groups > 0 ? ctx->sell_off.p : nullptr;
     a.sell_col = ctx->sell_col.p;
     a.sell_val = ctx->sell_val.p;

@@ -29,6 +29,7 @@
 //     padded to that length, so no loop carries a bounds test.
 //   * Reductions are warp shuffles plus one shared-memory exchange in a fixed
 //     order, so a launch is bitwise repeatable.
+#include <algorithm>
 #include <cfloat>
 #include <cmath>
 
@@ -287,13 +288,73 @@ __device__ __forceinline__ unsigned long long residual_max_bits(const ChainArgs 
     return mx;
 }
 
+// x <- x - S^T z, z = (S S^T)^+ S x: the reference's N (N^T x) written through
+// the residual (equal in exact arithmetic).  S x is summed in FP64 over the
+// same rows as the check and kept as FP32 hi + lo pairs in rr (m entries of
+// the staging buffer); z = (S S^T)^+ r runs in FP32 (a warp per row of the
+// pseudo-inverse, coalesced), whose relative error (~1e-7 times the condition
+// number) applies to the correction, not to x, which is at most of the size of
+// the residual's preimage; the update x_j -= sum_i S_ij z_i is FP64 (CSC).
+template <int BD>
+__device__ __forceinline__ void residual_form_reproject(const ChainArgs &a, double *xs, float2 *rr, float *zs,
+                                                        int tid) {
+    constexpr int NW = BD / 32;
+    const int lane = tid & 31, warp = tid >> 5;
+    const int m = a.m;
+    if (a.sell_off) {
+        for (int g = warp; g < a.sell_groups; g += NW) {
+            const int base = __ldg(a.sell_off + g);
+            const int len = (__ldg(a.sell_off + g + 1) - base) >> 5;
+            double acc = 0.0;
+#pragma unroll 4
+            for (int t = 0; t < len; ++t) {
+                const int q = base + (t << 5) + lane;
+                acc = fma(__ldg(a.sell_val + q), xs[__ldg(a.sell_col + q)], acc);
+            }
+            const int row = (g << 5) + lane;
+            if (row < m) {
+                const float hi = __double2float_rn(acc);
+                rr[row] = make_float2(hi, __double2float_rn(acc - (double)hi));
+            }
+        }
+    } else {
+        for (int row = tid; row < m; row += BD) {
+            double acc = 0.0;
+            const int q1 = __ldg(a.row_ptr + row + 1);
+            for (int q = __ldg(a.row_ptr + row); q < q1; ++q) acc = fma(__ldg(a.val + q), xs[__ldg(a.col_idx + q)], acc);
+            const float hi = __double2float_rn(acc);
+            rr[row] = make_float2(hi, __double2float_rn(acc - (double)hi));
+        }
+    }
+    __syncthreads();
+    for (int i = warp; i < m; i += NW) {
+        const float *Bi = a.pinv32 + (size_t)i * (size_t)m;
+        float acc = 0.0f;
+        for (int k = lane; k < m; k += 32) {
+            const float b = __ldg(Bi + k);
+            const float2 r = rr[k];
+            acc = fmaf(b, r.x, fmaf(b, r.y, acc));
+        }
+#pragma unroll
+        for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if (lane == 0) zs[i] = acc;
+    }
+    __syncthreads();
+    for (int j = tid; j < a.n; j += BD) {
+        double dl = 0.0;
+        const int q1 = __ldg(a.csc_ptr + j + 1);
+        for (int q = __ldg(a.csc_ptr + j); q < q1; ++q) dl = fma(__ldg(a.csc_val + q), (double)zs[__ldg(a.csc_row + q)], dl);
+        xs[j] -= dl;
+    }
+}
+
 }  // namespace
 
 constexpr int kTbl = 64;  // steps per refill of the step table
 
 // Shared memory of one CTA: xs, As, ws (NP doubles each; ws doubles as the
 // reprojection scratch), the step table and the reduction slots.
-inline size_t chain_smem_bytes_cfg(int np, int d, int bd) {
+__host__ __device__ inline size_t chain_smem_bytes_cfg(int np, int d, int bd) {
     (void)d;
     (void)bd;
     return sizeof(double) * 3 * (size_t)np + sizeof(StepEntry) * kTbl + 2 * sizeof(RedSlots) + 128;
@@ -315,6 +376,8 @@ __global__ void __launch_bounds__(BD, (BD <= 384 ? 2 : 1)) achr_chain_kernel(con
     uint64_t *bar = reinterpret_cast<uint64_t *>(rsb + 2);
     unsigned long long *cnt = reinterpret_cast<unsigned long long *>(bar + 1);  // CTA statistics, CNT_* slots
     int *exact_count = reinterpret_cast<int *>(cnt + 8);
+    // (S S^T)^+ r of the residual-form reprojection (m floats), when enabled
+    float *zs = reinterpret_cast<float *>(smem_raw + chain_smem_bytes_cfg(NP, a.d, BD));
 
     if (tid == 0) {
         mbar_init(bar, 1);
@@ -721,20 +784,25 @@ __global__ void __launch_bounds__(BD, (BD <= 384 ? 2 : 1)) achr_chain_kernel(con
                             inflight = false;
                         }
                         __syncthreads();
-                        const int n = a.n;
-                        for (int j = warp; j < a.d; j += NW) {
-                            const double *Nj = a.N + (size_t)j * (size_t)n;
-                            double acc = 0.0;
-                            for (int i = lane; i < n; i += 32) acc = fma(__ldg(Nj + i), xs[i], acc);
+                        if (a.pinv32) {
+                            residual_form_reproject<BD>(a, xs, reinterpret_cast<float2 *>(ws), zs, tid);
+                        } else {
+                            const int n = a.n;
+                            for (int j = warp; j < a.d; j += NW) {
+                                const double *Nj = a.N + (size_t)j * (size_t)n;
+                                double acc = 0.0;
+                                for (int i = lane; i < n; i += 32) acc = fma(__ldg(Nj + i), xs[i], acc);
 #pragma unroll
-                            for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-                            if (lane == 0) ys[j] = acc;
-                        }
-                        __syncthreads();
-                        for (int i = tid; i < n; i += BD) {
-                            double acc = 0.0;
-                            for (int j = 0; j < a.d; ++j) acc = fma(__ldg(a.N + (size_t)j * (size_t)n + i), ys[j], acc);
-                            xs[i] = acc;
+                                for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+                                if (lane == 0) ys[j] = acc;
+                            }
+                            __syncthreads();
+                            for (int i = tid; i < n; i += BD) {
+                                double acc = 0.0;
+                                for (int j = 0; j < a.d; ++j)
+                                    acc = fma(__ldg(a.N + (size_t)j * (size_t)n + i), ys[j], acc);
+                                xs[i] = acc;
+                            }
                         }
                         __syncthreads();
                         if (buf_col >= 0) {
@@ -855,14 +923,30 @@ __global__ void __launch_bounds__(BD, (BD <= 384 ? 2 : 1)) achr_chain_kernel(con
 // the grid; max_ctas < 0 launches one CTA per chain, leaving the balancing of
 // concurrent launches to the hardware CTA scheduler (batched models).
 template <int BD, int EPT>
-cudaError_t launch_cfg(const ChainArgs &a, cudaStream_t stream, int max_ctas, int *per_sm_out) {
-    const size_t smem = chain_smem_bytes_cfg(BD * EPT, a.d, BD);
+cudaError_t launch_cfg(const ChainArgs &a_in, cudaStream_t stream, int max_ctas, int *per_sm_out) {
+    ChainArgs a = a_in;
+    const size_t base = chain_smem_bytes_cfg(BD * EPT, a.d, BD);
+    // The residual-form reprojection keeps z (m floats) in shared memory and
+    // the residual in the staging buffer; it is used only when both fit
+    // without costing a resident CTA per SM.
+    const size_t zbytes = ((size_t)a.m * sizeof(float) + 15) & ~(size_t)15;
+    if (a.pinv32 && a.m > BD * EPT) a.pinv32 = nullptr;
+    size_t smem = base + (a.pinv32 ? zbytes : 0);
     cudaError_t e = cudaFuncSetAttribute(achr_chain_kernel<BD, EPT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smem);
+                                         (int)std::max(smem, base));
     if (e != cudaSuccess) return e;
     int per_sm = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, achr_chain_kernel<BD, EPT>, BD, smem);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, achr_chain_kernel<BD, EPT>, BD, base);
     if (e != cudaSuccess) return e;
+    if (a.pinv32) {
+        int per_sm_z = 0;
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_z, achr_chain_kernel<BD, EPT>, BD, smem);
+        if (e != cudaSuccess) return e;
+        if (per_sm_z < per_sm) {
+            a.pinv32 = nullptr;
+            smem = base;
+        }
+    }
     if (per_sm < 1) return cudaErrorInvalidConfiguration;
     if (per_sm_out) *per_sm_out = per_sm;
     if (a.P <= 0) return cudaSuccess;

@@ -44,6 +44,13 @@ void reproj_free(ReprojState *r);  // achr_reproject.cu
 
 }  // namespace achr
 
+struct achr_ctx;
+namespace achr {
+// (S S^T)^+ in FP32, rows and columns in the device row order, into ctx->pinv32
+// (achr_reproject.cu; builds the batched-reprojection operator on the way).
+achr_status build_pinv32(achr_ctx *ctx);
+}  // namespace achr
+
 struct achr_ctx {
     int n = 0, m = 0, W = 0, d = 0, ldw = 0, np = 0;
     float bound_err = 0.0f;
@@ -60,6 +67,10 @@ struct achr_ctx {
     achr::DevBuf<int> sell_off, sell_col;  // the same rows as sliced ELL (32-row groups)
     achr::DevBuf<double> sell_val;
     int sell_groups = 0;
+    std::vector<int> h_row_order;          // device row q is model row h_row_order[q]
+    achr::DevBuf<int> csc_ptr, csc_row;    // CSC of S with device (sorted) row indices
+    achr::DevBuf<double> csc_val;
+    achr::DevBuf<float> pinv32;            // (S S^T)^+ in FP32, device row order, m x m (empty: not built)
     achr::DevBuf<unsigned long long> counters;
     achr::ReprojState *reproj = nullptr;  // batched reprojection operator, built on first use
     achr::DevBuf<double> dirs;   // hit-and-run direction pool, n x n_dirs (leading dimension ldw)

@@ -48,6 +48,12 @@ struct ChainArgs {
     const int *sell_col;
     const double *sell_val;
     int sell_groups;
+    // Residual-form reprojection x <- x - S^T (S S^T)^+ S x: the pseudo-inverse
+    // in FP32 (m x m, device row order) and the CSC of S; pinv32 NULL: N (N^T x).
+    const float *pinv32;
+    const int *csc_ptr;
+    const int *csc_row;
+    const double *csc_val;
     const double *N;            // n x d column-major null-space basis (ld = n)
     double *out;                // n x P row-major block: out[i * ld_out + p]
     long long ld_out;

@@ -202,7 +202,17 @@ __global__ void split_matrix(int m, int kpad, const double *__restrict__ B, __nv
     Bl[t] = __double2bfloat16(v - (double)__bfloat162float(hi));
 }
 
-achr_status build_reproj(achr_ctx *ctx, ReprojState &R) {
+// (S S^T)^+ (column-major FP64) to FP32, rows and columns permuted to the
+// device row order of the chain kernel's S.
+__global__ void pinv32_kernel(int m, const int *__restrict__ order, const double *__restrict__ B,
+                              float *__restrict__ out) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)m * m) return;
+    const int i = (int)(t / m), k = (int)(t % m);
+    out[t] = (float)B[(long long)order[k] * m + order[i]];  // B symmetric, column-major
+}
+
+achr_status build_reproj(achr_ctx *ctx, ReprojState &R, bool want_pinv32 = false) {
     const int m = ctx->m, n = ctx->n;
     R.m = m;
     R.n = n;
@@ -303,6 +313,15 @@ achr_status build_reproj(achr_ctx *ctx, ReprojState &R) {
     const long long cnt = (long long)m * R.kpad;
     split_matrix<<<(unsigned)((cnt + 255) / 256), 256>>>(m, R.kpad, B.p, R.Bh.p, R.Bl.p);
     REPROJ_TRY(cudaGetLastError());
+    if (want_pinv32) {
+        DevBuf<int> ord;
+        REPROJ_TRY(ord.upload(ctx->h_row_order.data(), ctx->h_row_order.size()));
+        REPROJ_TRY(ctx->pinv32.alloc((size_t)m * m));
+        const long long mm = (long long)m * m;
+        pinv32_kernel<<<(unsigned)((mm + 255) / 256), 256>>>(m, ord.p, B.p, ctx->pinv32.p);
+        REPROJ_TRY(cudaGetLastError());
+        REPROJ_TRY(cudaDeviceSynchronize());
+    }
     REPROJ_TRY(cudaDeviceSynchronize());
     return ACHR_OK;
 }
@@ -345,6 +364,23 @@ dim3 residual_grid(int P, int kpad) {
 }
 
 }  // namespace
+
+achr_status build_pinv32(achr_ctx *ctx) {
+    if (ctx->pinv32.p) return ACHR_OK;
+    if ((int)ctx->h_row_order.size() != ctx->m) return set_err(ACHR_ERR_INVALID, "row order missing");
+    // Rebuild the operator with the FP32 copy requested (the first build frees B).
+    ReprojState *R = new (std::nothrow) ReprojState();
+    if (!R) return set_err(ACHR_ERR_NOMEM, "allocation failed");
+    const achr_status st = build_reproj(ctx, *R, true);
+    if (st != ACHR_OK) {
+        delete R;
+        return st;
+    }
+    reproj_free(ctx->reproj);
+    ctx->reproj = R;
+    return ACHR_OK;
+}
+
 }  // namespace achr
 
 using achr::ReprojState;

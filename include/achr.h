@@ -76,7 +76,12 @@ typedef struct {
     int32_t exact_ratio;      /* 1: evaluate every ratio-test candidate in FP64 (diagnostic, slower) */
     int32_t threads_per_chain;/* 0: chosen by size; else 32, 64, 128, 256, 320, 384 or 512 threads per chain
                                  (320 and 384 hold up to 3840 reactions) */
-    int32_t reserved;
+    int32_t reproject_form;   /* per-chain reprojection x <- N (N^T x) (ACHRCuda.cu:208-230) computed as
+                                 0: chosen by size (the residual form when n_rxns x null_dim >= 4e6),
+                                 1: N (N^T x) in FP64,
+                                 2: x - S^T (S S^T)^+ S x, the pseudo-inverse product in FP32 on the
+                                    residual (equal in exact arithmetic; m^2 FP32 instead of 4 n d FP64
+                                    operations); needs n_mets <= 8192 */
     double residual_tol;      /* 1e-9 (ACHRCuda.cu:338) */
     double max_min_tol;       /* 1e-9 (ACHRCuda.cu:505) */
     double u_tol;             /* 1e-9 (ACHRCuda.cu:508) */

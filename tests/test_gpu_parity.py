@@ -46,6 +46,21 @@ def test_points_match_oracle(sampler, oracle_mod, small_model, golden, steps):
     assert st["reprojections"] == rst["reprojections"]
 
 
+@pytest.mark.parametrize("steps", [11, 50])
+def test_residual_form_reprojection_matches_oracle(pkg, oracle_mod, small_model, golden, steps):
+    """reproject_form = 2: the per-chain reprojection as x - S^T (S S^T)^+ S x (pseudo-inverse
+    product in FP32 on the residual) gives the oracle's N (N^T x) points within the same tolerance;
+    the fixture's %f-rounded warmups make every check reproject."""
+    P = 64
+    with pkg.Sampler(small_model, golden["warmup"], reproject_form=2) as s:
+        s.set_null_space(golden["N"])
+        pts, st = s.sample(P, steps, seed=1234)
+    ref, rst = oracle_mod.sample(small_model, golden["warmup"], golden["N"], 1234, P, steps)
+    assert st["reprojections"] == rst["reprojections"] > 0
+    assert rel_err(pts, ref) <= REL_TOL
+    assert st["accepted"] == rst["accepted"] == P * steps and st["rejected"] == rst["rejected"]
+
+
 def test_golden_fixture_points(sampler, golden):
     pts, _ = sampler.sample(int(golden["chains"]), int(golden["steps"]), seed=int(golden["seed"]))
     assert rel_err(pts, golden["points"]) <= REL_TOL
