@@ -194,6 +194,33 @@ __device__ __forceinline__ unsigned long long shfl_u64(unsigned long long v, int
     return __shfl_xor_sync(0xffffffffu, v, o);
 }
 
+// Warp minima with the single-instruction integer reductions (redux.sync)
+// instead of five shuffle rounds: floats through an order-preserving key,
+// 64-bit keys as (high word, then low word among the lanes holding the high
+// minimum).
+__device__ __forceinline__ unsigned f32_key(float f) {
+    const unsigned b = __float_as_uint(f);
+    return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+__device__ __forceinline__ float key_f32(unsigned k) {
+    return __uint_as_float((k & 0x80000000u) ? (k & 0x7fffffffu) : ~k);
+}
+__device__ __forceinline__ float warp_min_f32(float v) {
+    return key_f32(__reduce_min_sync(0xffffffffu, f32_key(v)));
+}
+__device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long v) {
+    const unsigned hi = (unsigned)(v >> 32);
+    const unsigned mhi = __reduce_max_sync(0xffffffffu, hi);
+    const unsigned mlo = __reduce_max_sync(0xffffffffu, hi == mhi ? (unsigned)v : 0u);
+    return ((unsigned long long)mhi << 32) | mlo;
+}
+__device__ __forceinline__ unsigned long long warp_min_u64(unsigned long long v) {
+    const unsigned hi = (unsigned)(v >> 32);
+    const unsigned mhi = __reduce_min_sync(0xffffffffu, hi);
+    const unsigned mlo = __reduce_min_sync(0xffffffffu, hi == mhi ? (unsigned)v : 0xffffffffu);
+    return ((unsigned long long)mhi << 32) | mlo;
+}
+
 // Shared-memory exchange slots, two sets selected by attempt parity so that
 // consecutive attempts never overwrite slots another warp may still read.
 struct RedSlots {
@@ -566,12 +593,9 @@ __global__ void __launch_bounds__(BD, (BD <= 384 ? 2 : 1)) achr_chain_kernel(con
                     fl = 2 | 4;
                     my_lh = my_ll = -INFINITY;
                 }
-#pragma unroll
-                for (int o = 16; o; o >>= 1) {
-                    uh = fminf(uh, __shfl_xor_sync(0xffffffffu, uh, o));
-                    ul = fminf(ul, __shfl_xor_sync(0xffffffffu, ul, o));
-                    fl |= __shfl_xor_sync(0xffffffffu, fl, o);
-                }
+                uh = warp_min_f32(uh);
+                ul = warp_min_f32(ul);
+                fl = (int)__reduce_or_sync(0xffffffffu, (unsigned)fl);
                 if (lane == 0) {
                     rs->min2[warp] = make_float2(uh, ul);
                     rs->flag2[warp] = fl;
@@ -659,12 +683,9 @@ __global__ void __launch_bounds__(BD, (BD <= 384 ? 2 : 1)) achr_chain_kernel(con
                     }
                 }
                 if (nex) atomicAdd(exact_count, nex);
-#pragma unroll
-                for (int o = 16; o; o >>= 1) {
-                    kh = umin(kh, shfl_u64(kh, o));
-                    kl = umin(kl, shfl_u64(kl, o));
-                    anyv |= __shfl_xor_sync(0xffffffffu, anyv, o);
-                }
+                kh = warp_min_u64(kh);
+                kl = warp_min_u64(kl);
+                anyv = (int)__reduce_or_sync(0xffffffffu, (unsigned)anyv);
                 if (lane == 0) {
                     rs->min3[warp] = make_ulonglong2(kh, kl);
                     rs->flag3[warp] = anyv;
@@ -766,8 +787,7 @@ __global__ void __launch_bounds__(BD, (BD <= 384 ? 2 : 1)) achr_chain_kernel(con
                     __syncthreads();
                     if (tid == 0) ++cnt[CNT_CHECKS];
                     unsigned long long mx = residual_max_bits<BD>(a, xs, tid);
-#pragma unroll
-                    for (int o = 16; o; o >>= 1) mx = umax(mx, shfl_u64(mx, o));
+                    mx = warp_max_u64(mx);
                     if (lane == 0) rs->max4[warp] = mx;
                     __syncthreads();
                     mx = 0;
@@ -856,8 +876,7 @@ __global__ void __launch_bounds__(BD, (BD <= 384 ? 2 : 1)) achr_chain_kernel(con
             unsigned long long res = 0;
             for (int pass = 0; pass < 2; ++pass) {
                 unsigned long long mx = residual_max_bits<BD>(a, xs, tid);
-#pragma unroll
-                for (int o = 16; o; o >>= 1) mx = umax(mx, shfl_u64(mx, o));
+                mx = warp_max_u64(mx);
                 __syncthreads();
                 if (lane == 0) rs->max4[warp] = mx;
                 __syncthreads();
@@ -889,8 +908,7 @@ __global__ void __launch_bounds__(BD, (BD <= 384 ? 2 : 1)) achr_chain_kernel(con
                 viol = fmax(viol, fmax(lu.x - xi, xi - lu.y));
             }
             unsigned long long vb = (unsigned long long)__double_as_longlong(viol);
-#pragma unroll
-            for (int o = 16; o; o >>= 1) vb = umax(vb, shfl_u64(vb, o));
+            vb = warp_max_u64(vb);
             __syncthreads();
             if (lane == 0) rs->max4[warp] = vb;
             __syncthreads();
