@@ -190,10 +190,6 @@ __device__ __forceinline__ T umax(T a, T b) {
     return a > b ? a : b;
 }
 
-__device__ __forceinline__ unsigned long long shfl_u64(unsigned long long v, int o) {
-    return __shfl_xor_sync(0xffffffffu, v, o);
-}
-
 // Warp minima with the single-instruction integer reductions (redux.sync)
 // instead of five shuffle rounds: floats through an order-preserving key,
 // 64-bit keys as (high word, then low word among the lanes holding the high
