@@ -94,17 +94,22 @@ def bulk_ess(draws: np.ndarray) -> np.ndarray:
     return m * n / tau
 
 
-def summarize(draws: np.ndarray, frozen_tol: float = 1e-9) -> dict:
+def summarize(draws: np.ndarray, frozen_tol: float = 1e-9, exclude=None) -> dict:
     """min ESS, max R-hat and their parameters; draws (chains, draws, params).
 
     A parameter whose draws all lie within frozen_tol * max(1, |median|) of
     each other is frozen (a blocked reaction, or one pinned by the constraints
     and moving only by rounding): it has no meaningful ESS or R-hat and is
-    counted separately."""
+    counted separately.  exclude (boolean per parameter) marks parameters known
+    to be pinned -- for fluxes, those with one value in every warmup point --
+    which are left out even when rounding drift over a long run moves them
+    past frozen_tol."""
     x = np.asarray(draws, dtype=np.float64)
     flat = x.reshape(-1, x.shape[2])
     spread = flat.max(axis=0) - flat.min(axis=0)
     moving = spread > frozen_tol * np.maximum(1.0, np.abs(np.median(flat, axis=0)))
+    if exclude is not None:
+        moving &= ~np.asarray(exclude, dtype=bool)
     ess = np.full(x.shape[2], np.nan)
     rhat = np.full(x.shape[2], np.nan)
     if moving.any():

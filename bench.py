@@ -499,6 +499,11 @@ def run_batch(args):
     return 0
 
 
+def pinned_reactions(warm):
+    """Reactions with one value in every warmup point (blocked, or pinned at a bound)."""
+    return np.ptp(warm, axis=1) <= 1e-9 * np.maximum(1.0, np.abs(warm).max(axis=1))
+
+
 def dispersed_starts(warm, M, seed):
     """Over-dispersed starting points for R-hat: chain p starts at a random warmup point
     (seeded), with the centre accumulator of a fresh chain, (W) * centre of the warmups."""
@@ -563,7 +568,7 @@ def run_ess(args):
     starts = dispersed_starts(warm, M, args.seed + 5) if args.start == "warmup" else None
     draws, ms, acc_steps = ess_trace(smp, M, B, K, L, args.seed, stream, starts=starts)
     t0 = time.perf_counter()
-    summ = diag.summarize(draws)
+    summ = diag.summarize(draws, exclude=pinned_reactions(warm))
     diag_s = time.perf_counter() - t0
     line = {
         "metric": "min-ESS/s", "value": summ["min_ess"] / (ms * 1e-3), "unit": "effective samples/s",
@@ -676,7 +681,7 @@ def run_learned(args):
         if name == "learned":
             plain.precond_pool(args.precond_rank, s_par.data_ptr(), U_par.data_ptr(), args.pool, seed=args.seed + 11)
         draws, ms, steps = ess_trace(plain, M, B, K, L, args.seed + 101, stream, starts=starts)
-        summ = diag.summarize(draws)
+        summ = diag.summarize(draws, exclude=pinned_reactions(warm))
         out[name] = {"min_ess_per_s": summ["min_ess"] / (ms * 1e-3), "min_ess": summ["min_ess"],
                      "max_rhat": summ["max_rhat"], "median_rhat": summ["median_rhat"],
                      "rhat_q99": summ["rhat_q99"], "median_ess": summ["median_ess"], "sampling_ms": ms,

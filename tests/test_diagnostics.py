@@ -55,3 +55,13 @@ def test_frozen_parameter_excluded(diag):
     x[:, :, 1] = 7.0
     s = diag.summarize(x)
     assert s["params"] == 2 and s["frozen_params"] == 1
+
+
+def test_excluded_parameters_are_left_out(diag):
+    rng = np.random.default_rng(6)
+    x = rng.standard_normal((4, 300, 3))
+    x[0, :, 2] += 1e-6 * np.arange(300)  # a "pinned" flux drifting by rounding in one chain
+    s_all = diag.summarize(x)
+    s_ex = diag.summarize(x, exclude=[False, False, True])
+    assert s_all["params"] == 3 and s_ex["params"] == 2 and s_ex["frozen_params"] == 1
+    assert s_ex["max_rhat"] <= s_all["max_rhat"]
