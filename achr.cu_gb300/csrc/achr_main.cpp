@@ -10,6 +10,9 @@
 //   --null sts|svd      null-space construction (default sts, the reference's rule)
 //   --centre cuda|matlab  centre weights (ACHRCuda.cu:347-348 or ACHRSamplerMOD.m:174)
 //   --threads-per-chain N
+//   --check-period N    residual check every N steps (default 10, ACHRCuda.cu:325; 0 = never)
+//   --reproject nnt|residual  per-chain reprojection as N (N^T x) or through the residual
+//                       (default: chosen by model size)
 //   --writer-threads N  host threads formatting File<ii>
 //   --report path.json  write sampling statistics
 #include <cuda_runtime.h>
@@ -48,8 +51,8 @@ int main(int argc, char **argv) {
     if (argc < 6) {
         std::fprintf(stderr,
                      "usage: %s model.mps warmuppoints.csv nFiles nPoints nSteps [--seed S] [--mode reference|feasible]"
-                     " [--null sts|svd] [--centre cuda|matlab] [--threads-per-chain N] [--writer-threads N]"
-                     " [--report file.json]\n",
+                     " [--null sts|svd] [--centre cuda|matlab] [--threads-per-chain N] [--check-period N]"
+                     " [--reproject nnt|residual] [--writer-threads N] [--report file.json]\n",
                      argv[0]);
         return 2;
     }
@@ -89,6 +92,14 @@ int main(int argc, char **argv) {
         } else if (f == "--threads-per-chain") {
             if (!parse_int(need(), v)) return std::fprintf(stderr, "ACHRCuda: bad --threads-per-chain\n"), 2;
             opt.threads_per_chain = (int32_t)v;
+        } else if (f == "--check-period") {
+            if (!parse_int(need(), v) || v < 0) return std::fprintf(stderr, "ACHRCuda: bad --check-period\n"), 2;
+            opt.check_period = (int32_t)v;
+        } else if (f == "--reproject") {
+            std::string m = need();
+            if (m == "nnt") opt.reproject_form = 1;
+            else if (m == "residual") opt.reproject_form = 2;
+            else return std::fprintf(stderr, "ACHRCuda: bad --reproject\n"), 2;
         } else if (f == "--writer-threads") {
             if (!parse_int(need(), v)) return std::fprintf(stderr, "ACHRCuda: bad --writer-threads\n"), 2;
             writer_threads = (int)v;
