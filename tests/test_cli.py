@@ -31,6 +31,13 @@ def test_cli_bad_numbers(native, pkg, tmp_path):
     assert r.returncode == 2
 
 
+@pytest.mark.parametrize("flags", [["--reproject", "fast"], ["--check-period", "-1"], ["--mode", "x"],
+                                   ["--seed"], ["--bogus", "1"]])
+def test_cli_bad_flags(native, pkg, tmp_path, flags):
+    r = _run(pkg, [GOLDEN / "small.mps", GOLDEN / "small_warmup.csv", 1, 2, 2, *flags], tmp_path)
+    assert r.returncode == 2
+
+
 def test_cli_truncated_warmup(native, pkg, tmp_path):
     bad = tmp_path / "w.csv"
     bad.write_text("\n".join((GOLDEN / "small_warmup.csv").read_text().splitlines()[:10]) + "\n")
