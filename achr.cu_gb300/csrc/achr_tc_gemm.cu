@@ -12,13 +12,15 @@
 // no counterpart: its reprojection (ACHRcu/ACHRCuda.cu:208-230) is a per-chain
 // FP64 GEMV pair.
 //
-// One CTA computes one 128 x 256 tile with six warps:
+// A persistent CTA per SM computes 128 x 256 tiles with six warps:
 //   warp 0      one thread issues the TMA loads of A and B k-blocks (64 wide);
-//   warp 1      allocates 256 tensor-memory columns; one thread issues four
-//               128x256x16 MMAs per k-block and commits each stage back to
-//               the producer, then commits the accumulator to the epilogue;
-//   warps 2..5  read the accumulator (tcgen05.ld, 32 lanes each: warp w sees
-//               lanes 32 (w mod 4) .. +31) and store FP32 rows of C.
+//   warp 1      allocates 512 tensor-memory columns (two accumulators); one
+//               thread issues four 128x256x16 MMAs per k-block, commits each
+//               stage back to the producer and each finished accumulator to
+//               the epilogue;
+//   warps 2..5  read an accumulator (tcgen05.ld, 32 lanes each: warp w sees
+//               lanes 32 (w mod 4) .. +31), store FP32 rows of C and hand the
+//               accumulator back, while the MMAs of the next tile run.
 // Every mbarrier wait is bounded (2 s); on expiry the kernel records an error
 // bit, skips the rest of its work and still frees its tensor memory.
 #include <cuda.h>
@@ -26,6 +28,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <algorithm>
 #include <mutex>
 
 #include "achr_internal.h"
@@ -37,9 +40,9 @@ constexpr int kBM = 128, kBN = 256, kBK = 64, kStages = 4;
 constexpr unsigned kABytes = kBM * kBK * 2;  // 16 KB
 constexpr unsigned kBBytes = kBN * kBK * 2;  // 32 KB
 constexpr unsigned kStageBytes = kABytes + kBBytes;
-constexpr unsigned kTmemCols = 256;
+constexpr unsigned kTmemCols = 512;  // two 256-column FP32 accumulators
 constexpr int kThreads = 192;
-constexpr size_t kSmemBytes = (size_t)kStages * kStageBytes + 1024 + 128;
+constexpr size_t kSmemBytes = (size_t)kStages * kStageBytes + 1024 + 160;
 constexpr unsigned long long kTcWaitNs = 2000000000ull;
 
 // Instruction descriptor of tcgen05.mma kind::f16: D FP32 (bits 4-5 = 1),
@@ -150,6 +153,14 @@ struct GemmParams {
     unsigned long long gate_max;
 };
 
+__device__ __forceinline__ void bar_arrive(unsigned bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
+// Persistent: one CTA per SM walks the output tiles tile = blockIdx.x + k *
+// gridDim.x (M fastest, so CTAs working at the same time share B tiles in L2).
+// Two 256-column accumulators in tensor memory let the epilogue of one tile
+// overlap the MMAs of the next; the k-block ring runs on across tiles.
 __global__ void __launch_bounds__(kThreads, 1)
     tc_gemm_bf16_kernel(const __grid_constant__ CUtensorMap mA0, const __grid_constant__ CUtensorMap mA1,
                         const __grid_constant__ CUtensorMap mB0, const __grid_constant__ CUtensorMap mB1,
@@ -160,13 +171,15 @@ __global__ void __launch_bounds__(kThreads, 1)
     const unsigned base = (raw + 1023u) & ~1023u;  // 128-byte swizzle atoms repeat every 1024 B
     const unsigned bar_full = base + kStages * kStageBytes;
     const unsigned bar_empty = bar_full + 8 * kStages;
-    const unsigned bar_acc = bar_empty + 8 * kStages;
-    const unsigned tmem_slot = bar_acc + 8;
-    const unsigned *tmem_slot_ptr =
-        reinterpret_cast<const unsigned *>(smem_raw + (tmem_slot - raw));
+    const unsigned bar_accf = bar_empty + 8 * kStages;  // 2: accumulator b holds a finished tile
+    const unsigned bar_acce = bar_accf + 16;            // 2: the epilogue has drained accumulator b
+    const unsigned bar_done = bar_acce + 16;            // every MMA of this CTA has completed
+    const unsigned tmem_slot = bar_done + 8;
+    const unsigned *tmem_slot_ptr = reinterpret_cast<const unsigned *>(smem_raw + (tmem_slot - raw));
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int m0 = blockIdx.x * kBM, n0 = blockIdx.y * kBN;
+    const int m_tiles = (p.M + kBM - 1) / kBM;
+    const int tiles = m_tiles * ((p.N + kBN - 1) / kBN);
     const int kb_split = p.K / kBK;
     const int total = kb_split * p.nsplit;
 
@@ -175,7 +188,11 @@ __global__ void __launch_bounds__(kThreads, 1)
             bar_init(bar_full + 8 * s, 1);
             bar_init(bar_empty + 8 * s, 1);
         }
-        bar_init(bar_acc, 1);
+        for (int b = 0; b < 2; ++b) {
+            bar_init(bar_accf + 8 * b, 1);
+            bar_init(bar_acce + 8 * b, 4);  // one arrival per epilogue warp
+        }
+        bar_init(bar_done, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 1) {
@@ -192,57 +209,82 @@ __global__ void __launch_bounds__(kThreads, 1)
 
     if (warp == 0) {
         if (lane == 0) {
-            for (int kb = 0; kb < total; ++kb) {
-                const int s = kb % kStages;
-                const unsigned round = (unsigned)(kb / kStages);
-                if (kb >= kStages && !bar_wait(bar_empty + 8 * s, (round - 1u) & 1u)) {
-                    ok = false;
-                    break;
+            int it = 0;  // k-blocks issued by this CTA so far (the ring position)
+            for (int tile = blockIdx.x; tile < tiles && ok; tile += gridDim.x) {
+                const int m0 = (tile % m_tiles) * kBM, n0 = (tile / m_tiles) * kBN;
+                for (int kb = 0; kb < total; ++kb, ++it) {
+                    const int s = it % kStages;
+                    const unsigned round = (unsigned)(it / kStages);
+                    if (it >= kStages && !bar_wait(bar_empty + 8 * s, (round - 1u) & 1u)) {
+                        ok = false;
+                        break;
+                    }
+                    const int split = kb / kb_split;
+                    const int kx = (kb - split * kb_split) * kBK;
+                    const CUtensorMap *ma = split == 2 ? &mA1 : &mA0;
+                    const CUtensorMap *mb = split == 1 ? &mB1 : &mB0;
+                    const unsigned sa = base + (unsigned)s * kStageBytes;
+                    bar_expect_tx(bar_full + 8 * s, kStageBytes);
+                    tma_2d(sa, ma, kx, m0, bar_full + 8 * s);
+                    tma_2d(sa + kABytes, mb, kx, n0, bar_full + 8 * s);
                 }
-                const int split = kb / kb_split;
-                const int kx = (kb - split * kb_split) * kBK;
-                const CUtensorMap *ma = split == 2 ? &mA1 : &mA0;
-                const CUtensorMap *mb = split == 1 ? &mB1 : &mB0;
-                const unsigned sa = base + (unsigned)s * kStageBytes;
-                bar_expect_tx(bar_full + 8 * s, kStageBytes);
-                tma_2d(sa, ma, kx, m0, bar_full + 8 * s);
-                tma_2d(sa + kABytes, mb, kx, n0, bar_full + 8 * s);
             }
         }
     } else if (warp == 1) {
         if (lane == 0) {
-            for (int kb = 0; kb < total; ++kb) {
-                const int s = kb % kStages;
-                const unsigned round = (unsigned)(kb / kStages);
-                if (!bar_wait(bar_full + 8 * s, round & 1u)) {
+            int it = 0, t = 0;
+            for (int tile = blockIdx.x; tile < tiles && ok; tile += gridDim.x, ++t) {
+                const int b = t & 1;
+                const unsigned use = (unsigned)(t >> 1);
+                if (t >= 2 && !bar_wait(bar_acce + 8 * b, (use - 1u) & 1u)) {
                     ok = false;
                     break;
                 }
                 tc_fence_after();
-                const unsigned sa = base + (unsigned)s * kStageBytes;
+                const unsigned acc = tmem + (unsigned)(b * (int)kBN);
+                for (int kb = 0; kb < total; ++kb, ++it) {
+                    const int s = it % kStages;
+                    const unsigned round = (unsigned)(it / kStages);
+                    if (!bar_wait(bar_full + 8 * s, round & 1u)) {
+                        ok = false;
+                        break;
+                    }
+                    tc_fence_after();
+                    const unsigned sa = base + (unsigned)s * kStageBytes;
 #pragma unroll
-                for (int k = 0; k < kBK / 16; ++k)  // 16 BF16 = 32 bytes of K per MMA
-                    tc_mma(tmem, sw128_desc(sa + 32u * k), sw128_desc(sa + kABytes + 32u * k),
-                           (kb | k) != 0 ? 1u : 0u);
-                tc_commit(bar_empty + 8 * s);
+                    for (int k = 0; k < kBK / 16; ++k)  // 16 BF16 = 32 bytes of K per MMA
+                        tc_mma(acc, sw128_desc(sa + 32u * k), sw128_desc(sa + kABytes + 32u * k),
+                               (kb | k) != 0 ? 1u : 0u);
+                    tc_commit(bar_empty + 8 * s);
+                }
+                if (ok) tc_commit(bar_accf + 8 * b);
             }
-            tc_commit(bar_acc);  // also on the error path: the epilogue then frees nothing in flight
+            // Before tensor memory is freed: every MMA issued above has completed.
+            tc_commit(bar_done);
+            if (!bar_wait(bar_done, 0)) ok = false;
         }
         __syncwarp();
     } else {
         const int q = warp & 3;  // tensor-memory lanes 32q .. 32q + 31
-        bool got = bar_wait(bar_acc, 0);
-        got = __all_sync(0xffffffffu, got);
-        tc_fence_after();
-        if (!got) {
-            ok = false;
-        } else {
+        int t = 0;
+        for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x, ++t) {
+            const int b = t & 1;
+            const unsigned use = (unsigned)(t >> 1);
+            bool got = bar_wait(bar_accf + 8 * b, use & 1u);
+            got = __all_sync(0xffffffffu, got);
+            if (!got) {
+                ok = false;
+                break;
+            }
+            tc_fence_after();
+            const int m0 = (tile % m_tiles) * kBM, n0 = (tile / m_tiles) * kBN;
             const int row = m0 + q * 32 + lane;
             float *crow = p.C + (long long)row * p.ldc;
+            const unsigned acc = tmem + (unsigned)(b * (int)kBN) + ((unsigned)(q * 32) << 16);
 #pragma unroll 1
             for (int c = 0; c < kBN; c += 16) {
                 float v[16];
-                tmem_ld16(tmem + ((unsigned)(q * 32) << 16) + (unsigned)c, v);
+                tmem_ld16(acc + (unsigned)c, v);
                 const int col = n0 + c;
                 if (row < p.M && col < p.N) {
                     if (p.vec && col + 16 <= p.N) {
@@ -256,6 +298,9 @@ __global__ void __launch_bounds__(kThreads, 1)
                     }
                 }
             }
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) bar_arrive(bar_acce + 8 * b);
         }
     }
     if (!ok) atomicOr(p.err, (unsigned long long)ERR_TC_TIMEOUT);
@@ -306,8 +351,7 @@ const char *tc_gemm_check(const TcGemm &g) {
     if (g.lda % 8 || g.ldb % 8) return "operand leading dimensions must be multiples of 8 elements";
     const uintptr_t al = (uintptr_t)g.A0 | (uintptr_t)g.B0 | (g.nsplit == 3 ? ((uintptr_t)g.A1 | (uintptr_t)g.B1) : 0);
     if (al & 15u) return "operands must be 16-byte aligned";
-    if ((long long)(g.M + kBM - 1) / kBM > 2147483647ll || (g.N + kBN - 1) / kBN > 65535)
-        return "N too large for one launch";
+    if ((long long)((g.M + kBM - 1) / kBM) * ((g.N + kBN - 1) / kBN) > 2147483647ll) return "too many tiles";
     return nullptr;
 }
 
@@ -336,7 +380,15 @@ cudaError_t launch_tc_gemm(const TcGemm &g, unsigned long long *err, cudaStream_
     p.err = err;
     p.gate = g.gate;
     p.gate_max = g.gate_max;
-    dim3 grid((unsigned)((g.M + kBM - 1) / kBM), (unsigned)((g.N + kBN - 1) / kBN));
+    static int sms = 0;
+    if (sms == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms <= 0) sms = 1;
+    }
+    const long long tiles = (long long)((g.M + kBM - 1) / kBM) * ((g.N + kBN - 1) / kBN);
+    const unsigned grid = (unsigned)std::min<long long>(tiles, sms);
     tc_gemm_bf16_kernel<<<grid, kThreads, kSmemBytes, stream>>>(a0, a1, b0, b1, p);
     return cudaGetLastError();
 }
