@@ -165,13 +165,14 @@ __device__ __forceinline__ unsigned long long global_ns() {
     return t;
 }
 
-// Wait for the phase with the given parity to complete, giving up after kWaitNs.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, unsigned parity) {
+// Wait for the phase with the given parity to complete, giving up after limit_ns.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, unsigned parity,
+                                                  unsigned long long limit_ns = kWaitNs) {
     if (mbar_try_wait(bar, parity)) return true;
     const unsigned long long t0 = global_ns();
     for (;;) {
         if (mbar_try_wait(bar, parity)) return true;
-        if (global_ns() - t0 > kWaitNs) return false;
+        if (global_ns() - t0 > limit_ns) return false;
     }
 }
 
@@ -418,6 +419,7 @@ __global__ void __launch_bounds__(BD, (BD <= 384 ? 2 : 1)) achr_chain_kernel(con
     const float utol32 = a.utol32, mmt32 = a.mmt32;
     const unsigned long long res_tol_bits = (unsigned long long)__double_as_longlong(a.residual_tol);
     const bool hr = a.hit_and_run != 0;  // directions are the staged columns themselves (no centre)
+    const unsigned long long wait_ns = a.wait_ns ? a.wait_ns : kWaitNs;
     unsigned phase = 0, it = 0;
     bool failed = false;
     double worst_res = 0.0, worst_viol = 0.0;
@@ -500,7 +502,12 @@ __global__ void __launch_bounds__(BD, (BD <= 384 ? 2 : 1)) achr_chain_kernel(con
                     buf_col = r;
                 }
                 if (inflight) {
-                    if (!mbar_wait_bounded(bar, phase)) failed = true;
+                    if (!mbar_wait_bounded(bar, phase, wait_ns)) {
+                        // The column did not arrive within the caller's limit: record it,
+                        // then let the copy land (default limit) before the buffer is left.
+                        failed = true;
+                        mbar_wait_bounded(bar, phase);
+                    }
                     phase ^= 1u;
                     inflight = false;
                 }

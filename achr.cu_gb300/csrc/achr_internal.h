@@ -68,6 +68,7 @@ struct ChainArgs {
     int hit_and_run;            // 1: `warmup` holds directions; d = column r, no centre (A stays as loaded)
     double residual_tol, max_min_tol, u_tol, d_tol, feasibility_tol;
     unsigned long long *counters;  // CNT_SLOTS entries
+    unsigned long long wait_ns;    // limit of the wait for a staged column (0: the default, 2 s)
 };
 
 // Launch the persistent chain kernel; threads_per_chain = 0 picks the default

@@ -87,6 +87,10 @@ typedef struct {
     double u_tol;             /* 1e-9 (ACHRCuda.cu:508) */
     double d_tol;             /* 1e-14 (ACHRCuda.cu:512) */
     double feasibility_tol;   /* 1e-8: ||S v||_inf bound for emitted points in FEASIBLE mode */
+    int32_t wait_limit_ns;    /* bound on the chain kernel's wait for a staged warmup column; on expiry
+                                 the launch stops, drains its copy and returns ACHR_ERR_TIMEOUT
+                                 (0: the default of 2 s) */
+    int32_t reserved2;
 } achr_options;
 
 typedef struct {

@@ -1,0 +1,38 @@
+"""GPU: failure detection without a fault.  The chain kernel's wait for a staged
+warmup column is bounded; a limit of 1 ns makes the first wait run out (the copy
+cannot land that fast).  The launch records the timeout, lets its copy land,
+stops, and the call returns ACHR_ERR_TIMEOUT; the GPU context stays usable."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+TIMEOUT = 7  # ACHR_ERR_TIMEOUT
+
+
+def test_wait_limit_reports_timeout_and_context_stays_usable(pkg, small_model, golden, oracle_mod):
+    with pkg.Sampler(small_model, golden["warmup"], wait_limit_ns=1) as s:
+        s.set_null_space(golden["N"])
+        with pytest.raises(pkg.AchrError) as err:
+            s.sample(32, 20, seed=3)
+        assert err.value.status == TIMEOUT
+        with pytest.raises(pkg.AchrError):  # and again: nothing is left in a broken state
+            s.sample(32, 20, seed=3)
+    with pkg.Sampler(small_model, golden["warmup"]) as s2:
+        s2.set_null_space(golden["N"])
+        pts, st = s2.sample(32, 20, seed=3)
+    ref, _ = oracle_mod.sample(small_model, golden["warmup"], golden["N"], 3, 32, 20)
+    assert st["accepted"] == 32 * 20
+    assert np.abs(pts - ref).max() <= 1e-10 * max(1.0, np.abs(ref).max())
+
+
+def test_generous_wait_limit_changes_nothing(pkg, small_model, golden):
+    with pkg.Sampler(small_model, golden["warmup"], wait_limit_ns=500_000_000) as s:
+        s.set_null_space(golden["N"])
+        a, _ = s.sample(16, 15, seed=2)
+    with pkg.Sampler(small_model, golden["warmup"]) as s:
+        s.set_null_space(golden["N"])
+        b, _ = s.sample(16, 15, seed=2)
+    assert np.array_equal(a, b)
