@@ -537,9 +537,12 @@ __global__ void __launch_bounds__(BD, (BD <= 384 ? 2 : 1)) achr_chain_kernel(con
                 }
 #pragma unroll
                 for (int o = 16; o; o >>= 1) ss += __shfl_xor_sync(0xffffffffu, ss, o);
+                // Each thread timed its own wait: OR every lane's outcome so that
+                // the whole block leaves (or stays) together.
+                const bool warp_failed = __any_sync(0xffffffffu, failed);
                 if (lane == 0) {
                     rs->sum1[warp] = ss;
-                    rs->flag1[warp] = failed ? 1 : 0;
+                    rs->flag1[warp] = warp_failed ? 1 : 0;
                 }
                 __syncthreads();
                 ss = 0.0f;
@@ -806,7 +809,7 @@ __global__ void __launch_bounds__(BD, (BD <= 384 ? 2 : 1)) achr_chain_kernel(con
                             phase ^= 1u;
                             inflight = false;
                         }
-                        __syncthreads();
+                        if (__syncthreads_or(failed ? 1 : 0)) failed = true;  // block-uniform from here
                         if (a.pinv32) {
                             residual_form_reproject<BD>(a, xs, reinterpret_cast<float2 *>(ws), zs, tid);
                         } else {
