@@ -125,7 +125,6 @@ achr_status validate_options(const achr_options &o) {
     if (o.check_period < 0) return fail(ACHR_ERR_INVALID, "check_period must be >= 0 (0: no in-loop checks)");
     if (o.max_attempts <= 0) return fail(ACHR_ERR_INVALID, "max_attempts must be positive");
     if (o.reproject_form < 0 || o.reproject_form > 2) return fail(ACHR_ERR_INVALID, "reproject_form must be 0, 1 or 2");
-    if (o.wait_limit_ns < 0) return fail(ACHR_ERR_INVALID, "wait_limit_ns must be >= 0");
     if (o.centre_offset != 0 && o.centre_offset != 1) return fail(ACHR_ERR_INVALID, "centre_offset must be 0 or 1");
     if (o.threads_per_chain != 0 && o.threads_per_chain != 32 && o.threads_per_chain != 64 &&
         o.threads_per_chain != 128 && o.threads_per_chain != 256 && o.threads_per_chain != 320 &&
@@ -635,7 +634,9 @@ ChainArgs chain_args(const achr_ctx *ctx, uint64_t seed, uint64_t chain_offset, 
     a.A_out = nullptr;
     a.ld_state = 0;
     a.hit_and_run = 0;
-    a.wait_ns = ctx->opt.wait_limit_ns > 0 ? (unsigned long long)ctx->opt.wait_limit_ns : 0ull;
+    const long long wl = ctx->opt.wait_limit_ns;
+    a.wait_ns = wl != 0 ? (unsigned long long)(wl < 0 ? -wl : wl) : 0ull;
+    a.wait_never = wl < 0 ? 1 : 0;
     if (ctx->n_dirs > 0) {
         a.warmup = ctx->dirs.p;
         a.W = ctx->n_dirs;

@@ -400,11 +400,13 @@ __global__ void __launch_bounds__(BD, (BD <= 384 ? 2 : 1)) achr_chain_kernel(con
     uint64_t *bar = reinterpret_cast<uint64_t *>(rsb + 2);
     unsigned long long *cnt = reinterpret_cast<unsigned long long *>(bar + 1);  // CTA statistics, CNT_* slots
     int *exact_count = reinterpret_cast<int *>(cnt + 8);
+    uint64_t *never = reinterpret_cast<uint64_t *>(exact_count + 2);  // a barrier nothing arrives on
     // (S S^T)^+ r of the residual-form reprojection (m floats), when enabled
     float *zs = reinterpret_cast<float *>(smem_raw + chain_smem_bytes_cfg(NP, a.d, BD));
 
     if (tid == 0) {
         mbar_init(bar, 1);
+        mbar_init(never, 1);
         fence_mbar_init();
         *exact_count = 0;
         for (int c = 0; c < 8; ++c) cnt[c] = 0;
@@ -502,7 +504,9 @@ __global__ void __launch_bounds__(BD, (BD <= 384 ? 2 : 1)) achr_chain_kernel(con
                     buf_col = r;
                 }
                 if (inflight) {
-                    if (!mbar_wait_bounded(bar, phase, wait_ns)) {
+                    // a.wait_never (failure-detection test): the wait is on a barrier
+                    // that nothing completes, so it always runs out.
+                    if (!mbar_wait_bounded(a.wait_never ? never : bar, phase, wait_ns)) {
                         // The column did not arrive within the caller's limit: record it,
                         // then let the copy land (default limit) before the buffer is left.
                         failed = true;

@@ -69,6 +69,7 @@ struct ChainArgs {
     double residual_tol, max_min_tol, u_tol, d_tol, feasibility_tol;
     unsigned long long *counters;  // CNT_SLOTS entries
     unsigned long long wait_ns;    // limit of the wait for a staged column (0: the default, 2 s)
+    int wait_never;                // 1: that wait is on a barrier nothing completes (tests the timeout)
 };
 
 // Launch the persistent chain kernel; threads_per_chain = 0 picks the default

@@ -89,7 +89,9 @@ typedef struct {
     double feasibility_tol;   /* 1e-8: ||S v||_inf bound for emitted points in FEASIBLE mode */
     int32_t wait_limit_ns;    /* bound on the chain kernel's wait for a staged warmup column; on expiry
                                  the launch stops, drains its copy and returns ACHR_ERR_TIMEOUT
-                                 (0: the default of 2 s) */
+                                 (0: the default of 2 s).  A negative value -L is a test of that
+                                 path: the wait is on a barrier nothing completes and runs out after
+                                 L ns every time. */
     int32_t reserved2;
 } achr_options;
 

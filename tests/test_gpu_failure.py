@@ -1,7 +1,8 @@
 """GPU: failure detection without a fault.  The chain kernel's wait for a staged
-warmup column is bounded; a limit of 1 ns makes the first wait run out (the copy
-cannot land that fast).  The launch records the timeout, lets its copy land,
-stops, and the call returns ACHR_ERR_TIMEOUT; the GPU context stays usable."""
+warmup column is bounded; wait_limit_ns = -L makes that wait watch a barrier
+that nothing completes, so it runs out after L ns every time.  The launch
+records the timeout, lets its real copy land, stops, and the call returns
+ACHR_ERR_TIMEOUT; the GPU context stays usable."""
 from __future__ import annotations
 
 import numpy as np
@@ -13,7 +14,7 @@ TIMEOUT = 7  # ACHR_ERR_TIMEOUT
 
 
 def test_wait_limit_reports_timeout_and_context_stays_usable(pkg, small_model, golden, oracle_mod):
-    with pkg.Sampler(small_model, golden["warmup"], wait_limit_ns=1) as s:
+    with pkg.Sampler(small_model, golden["warmup"], wait_limit_ns=-1_000_000) as s:  # 1 ms
         s.set_null_space(golden["N"])
         with pytest.raises(pkg.AchrError) as err:
             s.sample(32, 20, seed=3)
