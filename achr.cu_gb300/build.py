@@ -69,7 +69,8 @@ def build(verbose: bool = False, force: bool = False) -> Path:
         obj = OUT / (Path(src).stem + ".o")
         objs.append(obj)
         jobs.append([cxx, *CXX_FLAGS, *inc, "-c", str(SRC / src), "-o", str(obj)])
-    srcs = [SRC / s for s in CU_SOURCES + CXX_SOURCES] + list(SRC.glob("*.cuh")) + list(SRC.glob("*.h"))
+    srcs = [SRC / s for s in CU_SOURCES + CXX_SOURCES + ["achr_main.cpp"]] + list(SRC.glob("*.cuh")) + \
+        list(SRC.glob("*.h"))
     srcs.append(INCLUDE / "achr.h")
     lib = library_path()
     newest = max(p.stat().st_mtime for p in srcs)
@@ -83,9 +84,10 @@ def build(verbose: bool = False, force: bool = False) -> Path:
     _run([nvcc, *ARCH, "-shared", "-o", str(lib), *map(str, objs), "-L", str(libdir),
           "-lcusolver", "-lcublas", "-lcudart", "-Xlinker", f"-rpath={libdir}"])
     main_obj = OUT / "achr_main.o"
-    _run([cxx, *CXX_FLAGS, *inc, "-I", str(cuda / "include"), "-c", str(SRC / "achr_main.cpp"), "-o", str(main_obj)])
-    _run([cxx, "-o", str(cli_path()), str(main_obj), "-L", str(OUT), "-lachr_gb300", "-L", str(libdir), "-lcudart",
-          f"-Wl,-rpath,{OUT}", f"-Wl,-rpath,{libdir}"])
+    _run([cxx, *CXX_FLAGS, "-pthread", *inc, "-I", str(cuda / "include"), "-c", str(SRC / "achr_main.cpp"), "-o",
+          str(main_obj)])
+    _run([cxx, "-pthread", "-o", str(cli_path()), str(main_obj), "-L", str(OUT), "-lachr_gb300", "-L", str(libdir),
+          "-lcudart", f"-Wl,-rpath,{OUT}", f"-Wl,-rpath,{libdir}"])
     if verbose:
         print(f"built {lib} and {cli_path()}")
     return lib

@@ -23,6 +23,7 @@
 #include <cstring>
 #include <ctime>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/achr.h"
@@ -167,19 +168,39 @@ int main(int argc, char **argv) {
     std::printf("Null space dimension is %d \n", d);
     std::printf("Null space done in %.5f seconds.\n", now_s() - t0);
 
-    std::vector<double> pts((size_t)n * (size_t)nPoints);
+    // Two host buffers: File<ii> is formatted and written by a writer thread
+    // while the GPU samples file ii + 1 (the reference samples and writes in
+    // turn, ACHRCuda.cu:736-756).
+    std::vector<double> pts[2];
+    pts[0].resize((size_t)n * (size_t)nPoints);
+    if (nFiles > 1) pts[1].resize((size_t)n * (size_t)nPoints);
+    std::thread writer;
+    bool write_ok = true;
+    std::string write_err;
+    auto join_writer = [&]() -> bool {
+        if (writer.joinable()) writer.join();
+        return write_ok;
+    };
+    auto fail_run = [&](const char *what) -> int {
+        join_writer();
+        achr_destroy(ctx);
+        achr_free(warm);
+        achr_free_model(&mb);
+        if (!write_ok) {
+            std::fprintf(stderr, "ACHRCuda: writing points: %s\n", write_err.c_str());
+            return 2;
+        }
+        return die(what);
+    };
     achr_stats total{};
     for (long long ii = 0; ii < nFiles; ++ii) {
         std::printf("File %lld\n", ii);
         std::fflush(stdout);
         achr_stats st{};
-        if (achr_sample(ctx, seed, (uint64_t)ii * (uint64_t)nPoints, (int32_t)nPoints, (int32_t)nSteps, pts.data(),
-                        &st) != ACHR_OK) {
-            achr_destroy(ctx);
-            achr_free(warm);
-            achr_free_model(&mb);
-            return die("sampling");
-        }
+        std::vector<double> &buf = pts[ii & 1];
+        if (achr_sample(ctx, seed, (uint64_t)ii * (uint64_t)nPoints, (int32_t)nPoints, (int32_t)nSteps, buf.data(),
+                        &st) != ACHR_OK)
+            return fail_run("sampling");
         total.accepted += st.accepted;
         total.rejected += st.rejected;
         total.checks += st.checks;
@@ -190,15 +211,17 @@ int main(int argc, char **argv) {
         if (st.max_residual > total.max_residual) total.max_residual = st.max_residual;
         if (st.max_bound_violation > total.max_bound_violation) total.max_bound_violation = st.max_bound_violation;
         total.kernel_ms += st.kernel_ms;
-        char name[64];
-        std::snprintf(name, sizeof name, "File%lld", ii);
-        if (achr_write_points_csv(name, pts.data(), n, (int32_t)nPoints, writer_threads) != ACHR_OK) {
-            achr_destroy(ctx);
-            achr_free(warm);
-            achr_free_model(&mb);
-            return die("writing points");
-        }
+        if (!join_writer()) return fail_run("writing points");
+        writer = std::thread([&, ii, bufp = buf.data()]() {
+            char name[64];
+            std::snprintf(name, sizeof name, "File%lld", ii);
+            if (achr_write_points_csv(name, bufp, n, (int32_t)nPoints, writer_threads) != ACHR_OK) {
+                write_ok = false;
+                write_err = achr_last_error();  // the message is per thread
+            }
+        });
     }
+    if (!join_writer()) return fail_run("writing points");
     const double elapsed = now_s() - t0;
     std::printf("Sampling done in %.5f seconds.\n", elapsed);
     if (total.stuck_chains)
