@@ -57,6 +57,7 @@ def parse_args():
                     help="min-ESS/s and max R-hat from trace snapshots: CHAINS chains, BURNIN steps, then SEGMENTS "
                          "snapshots STEPS steps apart")
     ap.add_argument("--gemm", type=int, metavar="CHAINS", help="time the tensor-core GEMM alone at this N")
+    ap.add_argument("--cli", action="store_true", help="wall time of the drop-in CLI on the 72 x 95 fixture")
     ap.add_argument("--learned", type=int, nargs=4, metavar=("CHAINS", "BURNIN", "SEGMENTS", "STEPS"),
                     help="learned-preconditioned hit-and-run against plain ACHR on this ESS schedule")
     ap.add_argument("--train-chains", type=int, default=65536)
@@ -869,8 +870,46 @@ def run_gemm(args):
     return 0
 
 
+def run_cli(args):
+    """The drop-in command line on the reference's smallest published configuration: a 72 x 95
+    model (the committed fixture; the paper's E. coli core has the same size), 190 warmup points
+    from the LP restatement, nFiles = 1, nPoints = 1000, nSteps = 1000.  Wall-clock seconds of the
+    whole process (start-up, MPS and CSV reading, null space, sampling, File0), the figure the
+    reference's paper quotes (2 s on a K40 for E. coli core, 42 s for MATLAB)."""
+    import tempfile
+
+    import __graft_entry__ as ge
+
+    pkg = ge.load_package()
+    pkg.lib()
+    golden = ROOT / "tests" / "golden"
+    times = []
+    with tempfile.TemporaryDirectory() as tmp:
+        for k in range(args.warmup + args.steps):
+            t0 = time.perf_counter()
+            r = subprocess.run([str(pkg.cli_path()), str(golden / "small.mps"), str(golden / "small_warmup.csv"), "1",
+                                "1000", "1000", "--seed", str(args.seed + k)], cwd=tmp, capture_output=True,
+                               text=True)
+            el = time.perf_counter() - t0
+            if r.returncode != 0:
+                raise SystemExit(f"ACHRCuda failed ({r.returncode}): {r.stderr[-400:]}")
+            if k >= args.warmup:
+                times.append(el)
+        size = (Path(tmp) / "File0").stat().st_size
+    wall = float(np.median(times))
+    line = {"metric": "wall seconds (CLI, 1 file x 1000 points x 1000 steps)", "value": wall, "unit": "s",
+            "higher_is_better": False, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "dtype": "f64",
+            "data": "synthetic 72 x 95 fixture (tests/golden)", "chain_steps_per_s": 1e6 / wall,
+            "file0_bytes": size, "runs_s": times,
+            "config": {"workload": "small CLI: ACHRCuda small.mps small_warmup.csv 1 1000 1000"}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     args = parse_args()
+    if args.cli:
+        return run_cli(args)
     if args.gemm:
         return run_gemm(args)
     if args.learned:
