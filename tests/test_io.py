@@ -10,7 +10,10 @@ import pytest
 
 from conftest import GOLDEN
 
-REF_PUTIDA = Path("/root/reference/VFWarmup/lib/P_Putida.mps")
+# The reference checkout's own fixture model; the test runs only where
+# ACHR_REFERENCE_DIR names a checkout of the reference project.
+_REF_DIR = os.environ.get("ACHR_REFERENCE_DIR")
+REF_PUTIDA = Path(_REF_DIR, "VFWarmup", "lib", "P_Putida.mps") if _REF_DIR else Path("")
 
 
 def test_read_golden_mps(native, pkg, golden):
@@ -60,7 +63,7 @@ def _independent_mps_parse(path):
     return len(rows), len(cols), trip, np.array([lb[c] for c in order]), np.array([ub[c] for c in order])
 
 
-@pytest.mark.skipif(not REF_PUTIDA.exists(), reason="reference checkout not present")
+@pytest.mark.skipif(not REF_PUTIDA.is_file(), reason="ACHR_REFERENCE_DIR does not name a reference checkout")
 def test_read_reference_putida_model(native, pkg):
     """The reference's own fixture model (VFWarmup/lib/P_Putida.mps): 911 rows, 1060 columns."""
     m = pkg.read_mps(REF_PUTIDA)
