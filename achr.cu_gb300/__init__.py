@@ -64,7 +64,7 @@ class Options(C.Structure):
         ("centre_offset", C.c_int32), ("exact_ratio", C.c_int32), ("threads_per_chain", C.c_int32),
         ("reproject_form", C.c_int32),
         ("residual_tol", C.c_double), ("max_min_tol", C.c_double), ("u_tol", C.c_double), ("d_tol", C.c_double),
-        ("feasibility_tol", C.c_double), ("wait_limit_ns", C.c_int32), ("reserved2", C.c_int32),
+        ("feasibility_tol", C.c_double), ("wait_limit_ns", C.c_int32), ("bracket_pass", C.c_int32),
     ]
 
 

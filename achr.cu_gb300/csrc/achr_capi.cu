@@ -87,6 +87,24 @@ __global__ void centre_kernel(int n, int W, int ldw, const double *__restrict__ 
     A0[i] = (double)(W + centre_offset) * c;
 }
 
+// Largest column norm of an n x K column-major matrix (one block per column),
+// as the bits of a non-negative double, maxed into *out_bits.
+__global__ void col_norm_max_kernel(int n, long long ld, const double *__restrict__ M,
+                                    unsigned long long *out_bits) {
+    __shared__ double part[32];
+    const double *col = M + (size_t)blockIdx.x * (size_t)ld;
+    double s = 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) s = fma(col[i], col[i], s);
+    for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += part[w];
+        atomicMax(out_bits, (unsigned long long)__double_as_longlong(sqrt(t)));
+    }
+}
+
 }  // namespace
 
 extern "C" {
@@ -126,6 +144,7 @@ achr_status validate_options(const achr_options &o) {
     if (o.max_attempts <= 0) return fail(ACHR_ERR_INVALID, "max_attempts must be positive");
     if (o.reproject_form < 0 || o.reproject_form > 2) return fail(ACHR_ERR_INVALID, "reproject_form must be 0, 1 or 2");
     if (o.centre_offset != 0 && o.centre_offset != 1) return fail(ACHR_ERR_INVALID, "centre_offset must be 0 or 1");
+    if (o.bracket_pass != 0 && o.bracket_pass != 1) return fail(ACHR_ERR_INVALID, "bracket_pass must be 0 or 1");
     if (o.threads_per_chain != 0 && o.threads_per_chain != 32 && o.threads_per_chain != 64 &&
         o.threads_per_chain != 128 && o.threads_per_chain != 256 && o.threads_per_chain != 320 &&
         o.threads_per_chain != 384 && o.threads_per_chain != 512)
@@ -397,6 +416,11 @@ achr_status achr_create(const achr_model *model, const double *warmup, int32_t n
         lu[i] = make_double2(model->lb[i], model->ub[i]);
     }
     ctx->bound_err = berr;
+    {
+        double bsq = 0.0;
+        for (int i = 0; i < n; ++i) bsq += std::max(model->lb[i] * model->lb[i], model->ub[i] * model->ub[i]);
+        ctx->box_norm = std::sqrt(bsq);
+    }
     for (int64_t k = 0; k < (int64_t)n * n_warmup; ++k)
         if (!std::isfinite(warmup[k])) return fail(ACHR_ERR_INVALID, "warmup points must be finite");
 
@@ -580,6 +604,20 @@ achr_status achr_sample_device(achr_ctx *ctx, uint64_t seed, uint64_t chain_offs
 
 namespace {
 
+// Upper bound of the FP32 candidacy threshold u_tol ||d|| (times its margin)
+// for the brackets formed before the block norm is known, from a bound on
+// ||d||; without a finite bound the brackets keep their own pass.
+void set_merged_bound(ChainArgs &a, double u_tol, double dnorm_max) {
+    const double t = u_tol * dnorm_max * 1.01;
+    if (std::isfinite(t) && t > 0.0 && t < 1e30) {
+        a.uthr_max = f32_up(t);
+        a.merged_ab = 1;
+    } else {
+        a.uthr_max = 0.0f;
+        a.merged_ab = 0;
+    }
+}
+
 ChainArgs chain_args(const achr_ctx *ctx, uint64_t seed, uint64_t chain_offset, int32_t n_points, int32_t n_steps,
                      double *d_points_out, int64_t ld_out) {
     ChainArgs a{};
@@ -601,6 +639,9 @@ ChainArgs chain_args(const achr_ctx *ctx, uint64_t seed, uint64_t chain_offset, 
     a.dtol_lo = f32_down(ctx->opt.d_tol) * (1.0f - 9.5367431640625e-07f);
     a.utol32 = (float)ctx->opt.u_tol;
     a.mmt32 = (float)ctx->opt.max_min_tol;
+    set_merged_bound(a, ctx->opt.u_tol, ctx->opt.bracket_pass == 1 ? INFINITY
+                                        : ctx->n_dirs > 0           ? ctx->dir_norm_max
+                                                                    : 2.0 * ctx->box_norm);
     a.row_ptr = ctx->rowptr.p;
     a.col_idx = ctx->colidx.p;
     a.val = ctx->val.p;
@@ -667,6 +708,19 @@ achr_status achr_set_directions(achr_ctx *ctx, const double *dirs, int64_t ld, i
                                sizeof(double) * ctx->n, n_dirs, cudaMemcpyDefault));
     ACHR_CUDA_TRY(ctx->zeros.alloc((size_t)ctx->np));
     ACHR_CUDA_TRY(cudaMemset(ctx->zeros.p, 0, sizeof(double) * (size_t)ctx->np));
+    {
+        // the longest direction bounds ||d|| for the brackets formed in phase A
+        DevBuf<unsigned long long> nb;
+        ACHR_CUDA_TRY(nb.alloc(1));
+        ACHR_CUDA_TRY(cudaMemset(nb.p, 0, sizeof(unsigned long long)));
+        col_norm_max_kernel<<<n_dirs, 256>>>(ctx->n, ctx->ldw, ctx->dirs.p, nb.p);
+        ACHR_CUDA_TRY(cudaGetLastError());
+        unsigned long long bits = 0;
+        ACHR_CUDA_TRY(cudaMemcpy(&bits, nb.p, sizeof bits, cudaMemcpyDeviceToHost));
+        double nm;
+        std::memcpy(&nm, &bits, sizeof nm);
+        ctx->dir_norm_max = nm;
+    }
     ctx->n_dirs = n_dirs;
     return ACHR_OK;
 }

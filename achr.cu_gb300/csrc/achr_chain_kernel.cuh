@@ -46,6 +46,10 @@ constexpr float kDn = 1.0f - 9.5367431640625e-07f;     // 1 - 2^-20
 constexpr float kAdUp = 1.0f + 4.76837158203125e-07f;  // 1 + 2^-21
 constexpr float kNormUp = 1.0f + 1e-5f;                // FP32 norm relative error margin
 constexpr float kNormDn = 1.0f - 1e-5f;
+// Lower bound of u_tol ||d|| from u_tol max|d_i|: the FP32 norm of a vector is
+// at least its largest element within (1 - 1e-6), and the threshold carries
+// the kNormDn margin; 0.999 leaves room for both and the products' rounding.
+constexpr float kProvDn = 0.999f;
 constexpr unsigned long long kWaitNs = 2000000000ull;  // bounded mbarrier wait: 2 s
 constexpr unsigned long long kInfBits = 0x7FF0000000000000ull;
 
@@ -421,6 +425,8 @@ __global__ void __launch_bounds__(BD, (BD <= 384 ? 2 : 1)) achr_chain_kernel(con
     const float utol32 = a.utol32, mmt32 = a.mmt32;
     const unsigned long long res_tol_bits = (unsigned long long)__double_as_longlong(a.residual_tol);
     const bool hr = a.hit_and_run != 0;  // directions are the staged columns themselves (no centre)
+    const bool merged = a.merged_ab != 0 && !a.exact_ratio;  // ratio-test brackets formed in phase A
+    const float uthr_max = a.uthr_max;
     const unsigned long long wait_ns = a.wait_ns ? a.wait_ns : kWaitNs;
     unsigned phase = 0, it = 0;
     bool failed = false;
@@ -519,7 +525,7 @@ __global__ void __launch_bounds__(BD, (BD <= 384 ? 2 : 1)) achr_chain_kernel(con
                 // Phase A: d = w_r - A / (W + t)  (reference ACHRCuda.cu:260-264);
                 // in hit-and-run mode the staged column is the direction itself.
                 double dreg[EPT];
-                float ss = 0.0f;
+                float ss = 0.0f, admax = 0.0f;
                 if (hr) {
 #pragma unroll
                     for (int k = 0; k < EPT; ++k) {
@@ -528,6 +534,7 @@ __global__ void __launch_bounds__(BD, (BD <= 384 ? 2 : 1)) achr_chain_kernel(con
                         dreg[k] = dk;
                         const float d32 = f64_to_f32_rz(dk);
                         ss = fmaf(d32, d32, ss);
+                        admax = fmaxf(admax, fabsf(d32));
                     }
                 } else {
 #pragma unroll
@@ -537,7 +544,32 @@ __global__ void __launch_bounds__(BD, (BD <= 384 ? 2 : 1)) achr_chain_kernel(con
                         dreg[k] = dk;
                         const float d32 = f64_to_f32_rz(dk);
                         ss = fmaf(d32, d32, ss);
+                        admax = fmaxf(admax, fabsf(d32));
                     }
+                }
+                // Phase B1 folded into phase A (merged): the brackets need ||d||
+                // only for the candidacy test |d_i| > u_tol ||d||, so they are
+                // formed now with a threshold interval that holds for any norm
+                // the block sum can give: above by uthr_max (checked after the
+                // reduction), below by u_tol times this thread's largest |d_i|.
+                // A coordinate certain under both is classified; any other
+                // gets a -inf lower end and is settled exactly in phase B2.
+                float uh = INFINITY, ul = INFINITY;
+                float my_lh = INFINITY, my_ll = INFINITY;  // this thread's smallest bracket lower ends
+                int fl = 0;
+                if (merged) {
+                    const float uthr_lo_p = utol32 * admax * kProvDn;
+#pragma unroll
+                    for (int k = 0; k < EPT; ++k) {
+                        const int i = tid + k * BD;
+                        float lo_h, lo_l;
+                        bracket(xs[i], dreg[k], __ldg(a.bnd + i), berr, dtol_hi, dtol_lo, uthr_max, uthr_lo_p, lo_h,
+                                lo_l, uh, ul, fl);
+                        my_lh = fminf(my_lh, lo_h);
+                        my_ll = fminf(my_ll, lo_l);
+                    }
+                    uh = warp_min_f32(uh);
+                    ul = warp_min_f32(ul);
                 }
 #pragma unroll
                 for (int o = 16; o; o >>= 1) ss += __shfl_xor_sync(0xffffffffu, ss, o);
@@ -547,6 +579,7 @@ __global__ void __launch_bounds__(BD, (BD <= 384 ? 2 : 1)) achr_chain_kernel(con
                 if (lane == 0) {
                     rs->sum1[warp] = ss;
                     rs->flag1[warp] = warp_failed ? 1 : 0;
+                    if (merged) rs->min2[warp] = make_float2(uh, ul);
                 }
                 __syncthreads();
                 ss = 0.0f;
@@ -555,6 +588,16 @@ __global__ void __launch_bounds__(BD, (BD <= 384 ? 2 : 1)) achr_chain_kernel(con
                 for (int w = 0; w < NW; ++w) {
                     ss += rs->sum1[w];
                     f1 |= rs->flag1[w];
+                }
+                if (merged) {
+                    uh = INFINITY;
+                    ul = INFINITY;
+#pragma unroll
+                    for (int w = 0; w < NW; ++w) {
+                        const float2 v = rs->min2[w];
+                        uh = fminf(uh, v.x);
+                        ul = fminf(ul, v.y);
+                    }
                 }
                 if (f1) {
                     failed = true;
@@ -586,131 +629,153 @@ __global__ void __launch_bounds__(BD, (BD <= 384 ? 2 : 1)) achr_chain_kernel(con
                 // Phase B1: FP32 brackets (reference ratio test ACHRCuda.cu:266-281)
                 const float uthr = utol32 * norm32;
                 const float uthr_hi = uthr * kNormUp, uthr_lo = uthr * kNormDn;
-                float uh = INFINITY, ul = INFINITY;
-                float my_lh = INFINITY, my_ll = INFINITY;  // this thread's smallest bracket lower ends
-                int fl = 0;
-                if (!a.exact_ratio) {
-#pragma unroll
-                    for (int k = 0; k < EPT; ++k) {
-                        const int i = tid + k * BD;
-                        float lo_h, lo_l;
-                        bracket(xs[i], dreg[k], __ldg(a.bnd + i), berr, dtol_hi, dtol_lo, uthr_hi, uthr_lo, lo_h, lo_l,
-                                uh, ul, fl);
-                        my_lh = fminf(my_lh, lo_h);  // NaN (not a candidate) is ignored, -inf (undecided) wins
-                        my_ll = fminf(my_ll, lo_l);
-                    }
+                if (merged && uthr_hi <= uthr_max) {
+                    fl = 0;  // the merged brackets stand; their flags are not used
                 } else {
-                    fl = 2 | 4;
-                    my_lh = my_ll = -INFINITY;
-                }
-                uh = warp_min_f32(uh);
-                ul = warp_min_f32(ul);
-                fl = (int)__reduce_or_sync(0xffffffffu, (unsigned)fl);
-                if (lane == 0) {
-                    rs->min2[warp] = make_float2(uh, ul);
-                    rs->flag2[warp] = fl;
-                }
-                __syncthreads();
-                uh = INFINITY;
-                ul = INFINITY;
-                fl = 0;
+                    // separate pass (merged: ||d|| exceeded the bound the merged brackets assumed)
+                    if (merged) __syncthreads();  // min2 of this attempt may still be read
+                    uh = INFINITY;
+                    ul = INFINITY;
+                    my_lh = INFINITY;
+                    my_ll = INFINITY;
+                    fl = 0;
+                    if (!a.exact_ratio) {
 #pragma unroll
-                for (int w = 0; w < NW; ++w) {
-                    const float2 v = rs->min2[w];
-                    uh = fminf(uh, v.x);
-                    ul = fminf(ul, v.y);
-                    fl |= rs->flag2[w];
+                        for (int k = 0; k < EPT; ++k) {
+                            const int i = tid + k * BD;
+                            float lo_h, lo_l;
+                            bracket(xs[i], dreg[k], __ldg(a.bnd + i), berr, dtol_hi, dtol_lo, uthr_hi, uthr_lo, lo_h,
+                                    lo_l, uh, ul, fl);
+                            my_lh = fminf(my_lh, lo_h);  // NaN (not a candidate) is ignored, -inf (undecided) wins
+                            my_ll = fminf(my_ll, lo_l);
+                        }
+                    } else {
+                        fl = 2 | 4;
+                        my_lh = my_ll = -INFINITY;
+                    }
+                    uh = warp_min_f32(uh);
+                    ul = warp_min_f32(ul);
+                    fl = (int)__reduce_or_sync(0xffffffffu, (unsigned)fl);
+                    if (lane == 0) {
+                        rs->min2[warp] = make_float2(uh, ul);
+                        rs->flag2[warp] = fl;
+                    }
+                    __syncthreads();
+                    uh = INFINITY;
+                    ul = INFINITY;
+                    fl = 0;
+#pragma unroll
+                    for (int w = 0; w < NW; ++w) {
+                        const float2 v = rs->min2[w];
+                        uh = fminf(uh, v.x);
+                        ul = fminf(ul, v.y);
+                        fl |= rs->flag2[w];
+                    }
                 }
 
                 // FP64 norm, only when some candidacy test sits inside the FP32
-                // norm's margin (or every candidate is evaluated in FP64).
+                // norm's margin (or every candidate is evaluated in FP64).  With
+                // merged brackets that is known only in phase B2, which then
+                // asks for it and runs once more.
                 double thr64 = 0.0;
                 bool have_norm64 = false;
                 double norm64 = 0.0;
-                if (fl & 4) {
-                    double s64 = 0.0;
+                unsigned long long kh, kl;
+                int anyv;
+                for (int b2 = 0;; ++b2) {
+                    if ((fl & 4) && !have_norm64) {
+                        double s64 = 0.0;
 #pragma unroll
-                    for (int k = 0; k < EPT; ++k) s64 = fma(dreg[k], dreg[k], s64);
+                        for (int k = 0; k < EPT; ++k) s64 = fma(dreg[k], dreg[k], s64);
 #pragma unroll
-                    for (int o = 16; o; o >>= 1) s64 += __shfl_xor_sync(0xffffffffu, s64, o);
-                    if (lane == 0) rs->sum5[warp] = s64;
-                    __syncthreads();
-                    s64 = 0.0;
+                        for (int o = 16; o; o >>= 1) s64 += __shfl_xor_sync(0xffffffffu, s64, o);
+                        if (lane == 0) rs->sum5[warp] = s64;
+                        __syncthreads();
+                        s64 = 0.0;
 #pragma unroll
-                    for (int w = 0; w < NW; ++w) s64 += rs->sum5[w];
-                    norm64 = sqrt(s64);
-                    have_norm64 = true;
-                    thr64 = a.u_tol * norm64;
-                }
+                        for (int w = 0; w < NW; ++w) s64 += rs->sum5[w];
+                        norm64 = sqrt(s64);
+                        have_norm64 = true;
+                        thr64 = a.u_tol * norm64;
+                    }
 
-                // Phase B2: FP64 evaluation of every coordinate whose bracket can
-                // hold a minimum, or whose candidacy the brackets left open.
-                unsigned long long kh = kInfBits, kl = kInfBits;
-                int anyv = 0, nex = 0;
-                unsigned mh = 0, ml = 0, mam = 0;  // bit k: contender for max / min step, undecided
-                // Only a thread whose own bracket lower ends reach the block minima
-                // can hold a contender; the others skip the second pass.
-                const bool mine = my_lh <= uh || my_ll <= ul;
-                if (!a.exact_ratio && mine) {
+                    // Phase B2: FP64 evaluation of every coordinate whose bracket can
+                    // hold a minimum, or whose candidacy the brackets left open.
+                    kh = kInfBits;
+                    kl = kInfBits;
+                    anyv = 0;
+                    int nex = 0, need64 = 0;
+                    unsigned mh = 0, ml = 0, mam = 0;  // bit k: contender for max / min step, undecided
+                    // Only a thread whose own bracket lower ends reach the block minima
+                    // can hold a contender; the others skip the second pass.
+                    const bool mine = my_lh <= uh || my_ll <= ul;
+                    if (!a.exact_ratio && mine) {
 #pragma unroll
-                    for (int k = 0; k < EPT; ++k) {
-                        const int i = tid + k * BD;
-                        float lo_h, lo_l, uh2 = INFINITY, ul2 = INFINITY;  // minima already known
-                        int fl2 = 0;
-                        bracket(xs[i], dreg[k], __ldg(a.bnd + i), berr, dtol_hi, dtol_lo, uthr_hi, uthr_lo, lo_h, lo_l,
-                                uh2, ul2, fl2);
-                        mh |= (lo_h <= uh ? 1u : 0u) << k;
-                        ml |= (lo_l <= ul ? 1u : 0u) << k;
-                        mam |= (lo_h == -INFINITY ? 1u : 0u) << k;
-                    }
-                } else if (a.exact_ratio) {
-                    mh = ml = mam = (EPT >= 32) ? 0xFFFFFFFFu : ((1u << EPT) - 1u);
-                }
-                for (unsigned m = mh | ml; m; m &= m - 1) {
-                    const int k = __ffs(m) - 1;
-                    const unsigned bit = 1u << k;
-                    const int i = tid + k * BD;
-                    ++nex;
-                    const double xi = xs[i], dk = pick(dreg, k);
-                    const double2 lu = ld_lbub(a.lbub + i);
-                    const double Dp = lu.y - xi, Dm = xi - lu.x;
-                    bool valid = true;
-                    if (mam & bit) {  // undecided: full FP64 candidacy test
-                        bool u_pass;
-                        if (have_norm64) {
-                            u_pass = abs_bits(dk) > (unsigned long long)__double_as_longlong(thr64);
-                        } else {
-                            u_pass = fabsf(f64_to_f32_rz(dk)) > uthr_hi;
+                        for (int k = 0; k < EPT; ++k) {
+                            const int i = tid + k * BD;
+                            float lo_h, lo_l, uh2 = INFINITY, ul2 = INFINITY;  // minima already known
+                            int fl2 = 0;
+                            bracket(xs[i], dreg[k], __ldg(a.bnd + i), berr, dtol_hi, dtol_lo, uthr_hi, uthr_lo, lo_h,
+                                    lo_l, uh2, ul2, fl2);
+                            mh |= (lo_h <= uh ? 1u : 0u) << k;
+                            ml |= (lo_l <= ul ? 1u : 0u) << k;
+                            mam |= (lo_h == -INFINITY ? 1u : 0u) << k;
                         }
-                        valid = Dp > a.d_tol && Dm > a.d_tol && u_pass;
+                    } else if (a.exact_ratio) {
+                        mh = ml = mam = (EPT >= 32) ? 0xFFFFFFFFu : ((1u << EPT) - 1u);
                     }
-                    if (valid) {
-                        const double ad = abs_int(dk);
-                        const bool pos = positive_int(dk);
-                        if (mh & bit) kh = umin(kh, (unsigned long long)__double_as_longlong((pos ? Dp : Dm) / ad));
-                        if (ml & bit) kl = umin(kl, (unsigned long long)__double_as_longlong((pos ? Dm : Dp) / ad));
-                        anyv = 1;
+                    for (unsigned m = mh | ml; m; m &= m - 1) {
+                        const int k = __ffs(m) - 1;
+                        const unsigned bit = 1u << k;
+                        const int i = tid + k * BD;
+                        ++nex;
+                        const double xi = xs[i], dk = pick(dreg, k);
+                        const double2 lu = ld_lbub(a.lbub + i);
+                        const double Dp = lu.y - xi, Dm = xi - lu.x;
+                        bool valid = true;
+                        if (mam & bit) {  // undecided: full FP64 candidacy test
+                            bool u_pass;
+                            if (have_norm64) {
+                                u_pass = abs_bits(dk) > (unsigned long long)__double_as_longlong(thr64);
+                            } else {
+                                const float ad32 = fabsf(f64_to_f32_rz(dk));
+                                // inside the FP32 norm's margin: settled with the FP64 norm
+                                if (!(ad32 > uthr_hi) && !(ad32 * kAdUp < uthr_lo)) need64 = 1;
+                                u_pass = ad32 > uthr_hi;
+                            }
+                            valid = Dp > a.d_tol && Dm > a.d_tol && u_pass;
+                        }
+                        if (valid) {
+                            const double ad = abs_int(dk);
+                            const bool pos = positive_int(dk);
+                            if (mh & bit) kh = umin(kh, (unsigned long long)__double_as_longlong((pos ? Dp : Dm) / ad));
+                            if (ml & bit) kl = umin(kl, (unsigned long long)__double_as_longlong((pos ? Dm : Dp) / ad));
+                            anyv = 1;
+                        }
                     }
-                }
-                if (nex) atomicAdd(exact_count, nex);
-                kh = warp_min_u64(kh);
-                kl = warp_min_u64(kl);
-                anyv = (int)__reduce_or_sync(0xffffffffu, (unsigned)anyv);
-                if (lane == 0) {
-                    rs->min3[warp] = make_ulonglong2(kh, kl);
-                    rs->flag3[warp] = anyv;
-                }
-                __syncthreads();
-                kh = kInfBits;
-                kl = kInfBits;
-                anyv = 0;
+                    if (nex) atomicAdd(exact_count, nex);
+                    kh = warp_min_u64(kh);
+                    kl = warp_min_u64(kl);
+                    anyv = (int)__reduce_or_sync(0xffffffffu, (unsigned)(anyv | (need64 << 1)));
+                    if (lane == 0) {
+                        rs->min3[warp] = make_ulonglong2(kh, kl);
+                        rs->flag3[warp] = anyv;
+                    }
+                    __syncthreads();
+                    kh = kInfBits;
+                    kl = kInfBits;
+                    anyv = 0;
 #pragma unroll
-                for (int w = 0; w < NW; ++w) {
-                    const ulonglong2 v = rs->min3[w];
-                    kh = umin(kh, v.x);
-                    kl = umin(kl, v.y);
-                    anyv |= rs->flag3[w];
+                    for (int w = 0; w < NW; ++w) {
+                        const ulonglong2 v = rs->min3[w];
+                        kh = umin(kh, v.x);
+                        kl = umin(kl, v.y);
+                        anyv |= rs->flag3[w];
+                    }
+                    if (!(anyv & 2) || have_norm64) break;
+                    fl |= 4;  // a contender's candidacy needs the FP64 norm: evaluate again with it
                 }
+                anyv &= 1;
                 if (!anyv) {  // no candidate: rejection (see ACHRCuda.cu:283-288)
                     if (tid == 0) ++cnt[CNT_REJECTED];
                     continue;

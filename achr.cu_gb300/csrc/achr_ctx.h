@@ -54,6 +54,10 @@ achr_status build_pinv32(achr_ctx *ctx);
 struct achr_ctx {
     int n = 0, m = 0, W = 0, d = 0, ldw = 0, np = 0;
     float bound_err = 0.0f;
+    // sqrt(sum_i max(lb_i^2, ub_i^2)): every point and centre of a chain lies in
+    // the box, so ||w - c|| <= 2 box_norm (inf when a bound is infinite)
+    double box_norm = 0.0;
+    double dir_norm_max = 0.0;  // largest norm of a hit-and-run direction
     double tuned_rate = 0.0;  // chain-steps per ms on the whole GPU with the tuned configuration (0: not measured)
     int device = 0;
     achr_options opt{};

@@ -39,6 +39,12 @@ struct ChainArgs {
     float bound_err;            // max |lb - float(lb)|, |ub - float(ub)| over finite bounds, rounded up
     float dtol_hi, dtol_lo;     // FP32 brackets of d_tol (1 +- 2^-20)
     float utol32, mmt32;        // u_tol and max_min_tol in FP32
+    // merged_ab = 1: the FP32 ratio-test brackets are formed in the same pass as
+    // d, before the block knows ||d||, with the candidacy threshold bounded by
+    // uthr_max >= u_tol ||d|| (from the box or the direction pool); the kernel
+    // falls back to a separate bracket pass on any step whose threshold exceeds it.
+    int merged_ab;
+    float uthr_max;
     const int *row_ptr;         // CSR of S (m + 1)
     const int *col_idx;
     const double *val;

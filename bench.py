@@ -75,9 +75,17 @@ def parse_args():
                     help="re-fit the preconditioner this many times on the learned sampler's own samples")
     ap.add_argument("--large-chains", type=int, default=262_144, help="chains of the large workload")
     ap.add_argument("--large-steps", type=int, default=200, help="timed steps of the large workload")
+    ap.add_argument("--threads-per-chain", type=int, default=0, help="chain-kernel block size (0: by model size)")
+    ap.add_argument("--bracket-pass", type=int, choices=[0, 1], default=0,
+                    help="0: ratio-test brackets formed with the direction; 1: a separate pass")
     ap.add_argument("--profile-case", type=int, nargs=2, metavar=("CHAINS", "STEPS"),
                     help="run two launches of CHAINS x STEPS of the workload and print their times (ncu captures)")
     return ap.parse_args()
+
+
+def sampler_options(args):
+    """Chain-kernel options from the command line (defaults: chosen by the library)."""
+    return {"threads_per_chain": args.threads_per_chain, "bracket_pass": args.bracket_pass}
 
 
 def dist_info():
@@ -280,7 +288,7 @@ def run_gpu(args):
     chain_base, _ = sharding.chain_block(rank, world, P)  # weak scaling: every rank runs its own P chains
 
     t_setup = time.perf_counter()
-    smp = pkg.Sampler(model, warm)
+    smp = pkg.Sampler(model, warm, **sampler_options(args))
     setup_s = time.perf_counter() - t_setup
     stream = torch.cuda.current_stream()
     out = torch.empty((n, P), dtype=torch.float64, device="cuda")
@@ -332,7 +340,7 @@ def run_gpu(args):
         for k in range(max(1, args.steps)):
             torch.cuda.synchronize()
             t0 = time.perf_counter()
-            with pkg.Sampler(model, wnp) as s2:
+            with pkg.Sampler(model, wnp, **sampler_options(args)) as s2:
                 s2.sample(P, T, seed=args.seed + 2000 + k, chain_offset=chain_base, out=host_out.numpy())
             torch.cuda.synchronize()
             e2e_times.append(time.perf_counter() - t0)
@@ -356,7 +364,8 @@ def run_gpu(args):
         "config": {"workload": f"{args.workload}: {spec.n_mets}x{spec.n_rxns} synthetic model, W={warm.shape[1]}, "
                                f"{P} chains x {T} steps per GPU, mode=reference",
                    "global_batch": world * P, "seq_len": T, "parallelism": f"chains sharded over {world} GPU(s)",
-                   "l2": "inputs exceed L2 (warmup matrix 224 MB > 129 MB); no flush"},
+                   "l2": "inputs exceed L2 (warmup matrix 224 MB > 129 MB); no flush",
+                   "options": sampler_options(args)},
         "gpu_launches": args.steps,
         "roofline": roofline,
         "cpu_baseline": cpu,
@@ -386,7 +395,7 @@ def run_profile_case(args):
     synth = importlib.import_module("achr_gb300.synthetic")
     spec, model, S, warm, _, _ = build_inputs(args.workload, pkg, synth)
     P, T = args.profile_case
-    smp = pkg.Sampler(model, warm)
+    smp = pkg.Sampler(model, warm, **sampler_options(args))
     out = torch.empty((spec.n_rxns, P), dtype=torch.float64, device="cuda")
     stream = torch.cuda.current_stream().cuda_stream
     for k in range(2):

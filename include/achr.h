@@ -92,7 +92,11 @@ typedef struct {
                                  (0: the default of 2 s).  A negative value -L is a test of that
                                  path: the wait is on a barrier nothing completes and runs out after
                                  L ns every time. */
-    int32_t reserved2;
+    int32_t bracket_pass;     /* FP32 ratio-test brackets (ACHRCuda.cu:266-281): 0: formed in the same pass
+                                 as the direction, before its norm is known, with the candidacy threshold
+                                 bounded through the box (or the longest hit-and-run direction); a step
+                                 whose threshold exceeds the bound, or a model with an infinite bound,
+                                 uses a separate pass.  1: always a separate pass.  Results are equal. */
 } achr_options;
 
 typedef struct {

@@ -73,7 +73,7 @@ def test_create_validates_before_gpu_work(native, pkg):
     wp = warm.ctypes.data_as(C.POINTER(C.c_double))
     ctx = C.c_void_p()
     for field, value in (("check_period", -1), ("reproject_form", 3), ("threads_per_chain", 100),
-                         ("max_attempts", 0), ("centre_offset", 2), ("mode", 7)):
+                         ("max_attempts", 0), ("centre_offset", 2), ("mode", 7), ("bracket_pass", 2)):
         o = pkg.default_options()
         setattr(o, field, value)
         assert native.achr_create(C.byref(mdl), wp, 1, C.byref(o), C.byref(ctx)) == 1, field
