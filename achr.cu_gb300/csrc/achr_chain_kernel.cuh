@@ -23,6 +23,9 @@
 //     ratio in FP32 with rigorous error bounds and evaluates in FP64 only the
 //     coordinates whose bracket can hold the minimum; clipping and the min/max
 //     reductions compare FP64 values as integers (order-preserving keys).
+//   * The brackets are formed in the same pass as d, before the block knows
+//     ||d||, so one block reduction serves the norm and the bracket minima
+//     (two barriers per accepted step: that one and the exact minima's).
 //   * Per-step scalars (warmup index, step uniform, 1/(W+t)) come from a
 //     shared-memory table that the CTA refills once every BD steps.
 //   * The element loops are unrolled over compile-time BD x EPT with arrays
@@ -405,6 +408,8 @@ __global__ void __launch_bounds__(BD, (BD <= 384 ? 2 : 1)) achr_chain_kernel(con
     unsigned long long *cnt = reinterpret_cast<unsigned long long *>(bar + 1);  // CTA statistics, CNT_* slots
     int *exact_count = reinterpret_cast<int *>(cnt + 8);
     uint64_t *never = reinterpret_cast<uint64_t *>(exact_count + 2);  // a barrier nothing arrives on
+    // largest residual and bound violation of the CTA's emitted points (bits of non-negative doubles)
+    unsigned long long *worst = reinterpret_cast<unsigned long long *>(never + 1);
     // (S S^T)^+ r of the residual-form reprojection (m floats), when enabled
     float *zs = reinterpret_cast<float *>(smem_raw + chain_smem_bytes_cfg(NP, a.d, BD));
 
@@ -414,6 +419,7 @@ __global__ void __launch_bounds__(BD, (BD <= 384 ? 2 : 1)) achr_chain_kernel(con
         fence_mbar_init();
         *exact_count = 0;
         for (int c = 0; c < 8; ++c) cnt[c] = 0;
+        worst[0] = worst[1] = 0;
     }
     // The TMA copy fills ws[0, ldw); the padding beyond stays zero.
 #pragma unroll
@@ -423,17 +429,16 @@ __global__ void __launch_bounds__(BD, (BD <= 384 ? 2 : 1)) achr_chain_kernel(con
     const unsigned col_bytes = (unsigned)(sizeof(double) * (size_t)a.ldw);
     const float dtol_hi = a.dtol_hi, dtol_lo = a.dtol_lo, berr = a.bound_err;
     const float utol32 = a.utol32, mmt32 = a.mmt32;
-    const unsigned long long res_tol_bits = (unsigned long long)__double_as_longlong(a.residual_tol);
     const bool hr = a.hit_and_run != 0;  // directions are the staged columns themselves (no centre)
     const bool merged = a.merged_ab != 0 && !a.exact_ratio;  // ratio-test brackets formed in phase A
     const float uthr_max = a.uthr_max;
-    const unsigned long long wait_ns = a.wait_ns ? a.wait_ns : kWaitNs;
     unsigned phase = 0, it = 0;
     bool failed = false;
-    double worst_res = 0.0, worst_viol = 0.0;
 
-    for (long long p = blockIdx.x; p < a.P && !failed; p += gridDim.x) {
-        const unsigned long long chain = a.chain_offset + (unsigned long long)p;
+    // (Scalars that stay constant over a launch are read from the kernel
+    // parameters where they are used rather than held in registers.)
+    for (int p = blockIdx.x; p < a.P && !failed; p = (int)min((long long)p + gridDim.x, (long long)a.P)) {
+#define ACHR_CHAIN_ID (a.chain_offset + (unsigned long long)p)
         if (a.x_in) {  // resume: the chain's point and centre accumulator after step0 steps
 #pragma unroll
             for (int k = 0; k < EPT; ++k) {
@@ -450,7 +455,7 @@ __global__ void __launch_bounds__(BD, (BD <= 384 ? 2 : 1)) achr_chain_kernel(con
                 As[i] = a.A0[i];
             }
         }
-        long long buf_col = -1;
+        int buf_col = -1;
         bool inflight = false, any_accepted = a.x_in != nullptr, stuck = false;
         const int s_end = a.step0 + a.T;
         // The reference checks when the step count is a multiple of the period
@@ -466,7 +471,7 @@ __global__ void __launch_bounds__(BD, (BD <= 384 ? 2 : 1)) achr_chain_kernel(con
                 for (int e = tid; e < kTbl; e += BD) {
                     const int st = s + e;
                     if (st < s_end) {
-                        const Philox4 pd = step_draw(a.seed, chain, (uint32_t)st, 0u);
+                        const Philox4 pd = step_draw(a.seed, ACHR_CHAIN_ID, (uint32_t)st, 0u);
                         StepEntry en;
                         en.U = step_uniform(pd);
                         en.inv = 1.0 / (double)(a.W + st + a.centre_offset);
@@ -477,18 +482,17 @@ __global__ void __launch_bounds__(BD, (BD <= 384 ? 2 : 1)) achr_chain_kernel(con
                 }
                 __syncthreads();
             }
-            const StepEntry te = tbl[s - tbase];
-            const double ninv = -te.inv;
-            const double U = te.U;
+            // this step's table entry (its fields are read where they are used)
+            const StepEntry *te = tbl + (s - tbase);
             for (int att = 0;; ++att, ++it) {
                 if (att >= a.max_attempts) {
                     stuck = true;
                     break;
                 }
                 RedSlots *rs = rsb + (it & 1u);
-                const long long r = att == 0
-                                        ? (long long)te.idx
-                                        : (long long)warmup_index(step_draw(a.seed, chain, (uint32_t)s, (uint32_t)att),
+                const int r = att == 0
+                                  ? (int)te->idx
+                                  : (int)warmup_index(step_draw(a.seed, ACHR_CHAIN_ID, (uint32_t)s, (uint32_t)att),
                                                                   (uint32_t)a.W);
                 if (buf_col != r) {
                     if (inflight) {
@@ -512,7 +516,7 @@ __global__ void __launch_bounds__(BD, (BD <= 384 ? 2 : 1)) achr_chain_kernel(con
                 if (inflight) {
                     // a.wait_never (failure-detection test): the wait is on a barrier
                     // that nothing completes, so it always runs out.
-                    if (!mbar_wait_bounded(a.wait_never ? never : bar, phase, wait_ns)) {
+                    if (!mbar_wait_bounded(a.wait_never ? never : bar, phase, a.wait_ns ? a.wait_ns : kWaitNs)) {
                         // The column did not arrive within the caller's limit: record it,
                         // then let the copy land (default limit) before the buffer is left.
                         failed = true;
@@ -537,6 +541,7 @@ __global__ void __launch_bounds__(BD, (BD <= 384 ? 2 : 1)) achr_chain_kernel(con
                         admax = fmaxf(admax, fabsf(d32));
                     }
                 } else {
+                    const double ninv = -te->inv;
 #pragma unroll
                     for (int k = 0; k < EPT; ++k) {
                         const int i = tid + k * BD;
@@ -607,10 +612,10 @@ __global__ void __launch_bounds__(BD, (BD <= 384 ? 2 : 1)) achr_chain_kernel(con
 
                 // Prefetch the next step's warmup column while this one is tested.
                 if (s + 1 < s_end) {
-                    const long long rn =
+                    const int rn =
                         (s + 1 - tbase < kTbl)
-                            ? (long long)tbl[s + 1 - tbase].idx
-                            : (long long)warmup_index(step_draw(a.seed, chain, (uint32_t)(s + 1), 0u), (uint32_t)a.W);
+                            ? (int)tbl[s + 1 - tbase].idx
+                            : (int)warmup_index(step_draw(a.seed, ACHR_CHAIN_ID, (uint32_t)(s + 1), 0u), (uint32_t)a.W);
                     if (rn != buf_col && rn >= 0 && rn < a.W) {
                         if (tid == 0) {
                             fence_proxy_async_smem();
@@ -818,7 +823,7 @@ __global__ void __launch_bounds__(BD, (BD <= 384 ? 2 : 1)) achr_chain_kernel(con
                     continue;
                 }
                 // t / ||d|| with t = U (max - min) + min (reference ACHRCuda.cu:314)
-                const double sstep = fma(U, qh + ql, -ql);
+                const double sstep = fma(te->U, qh + ql, -ql);
 
                 // Phase C: x = prev + t u (ACHRCuda.cu:242-249), residual check every
                 // check_period steps (:325-344), clip + centre (:193-206, :347-350).
@@ -868,7 +873,7 @@ __global__ void __launch_bounds__(BD, (BD <= 384 ? 2 : 1)) achr_chain_kernel(con
                     mx = 0;
 #pragma unroll
                     for (int w = 0; w < NW; ++w) mx = umax(mx, rs->max4[w]);
-                    if (mx > res_tol_bits) {
+                    if (mx > (unsigned long long)__double_as_longlong(a.residual_tol)) {
                         // x <- N (N^T x) in FP64 (reference reprojectPoint(2), ACHRCuda.cu:208-230).
                         // The scratch is ws: let the prefetched column land, use the
                         // buffer, then fetch the column again.
@@ -990,14 +995,17 @@ __global__ void __launch_bounds__(BD, (BD <= 384 ? 2 : 1)) achr_chain_kernel(con
             vb = 0;
 #pragma unroll
             for (int w = 0; w < NW; ++w) vb = umax(vb, rs->max4[w]);
-            worst_res = fmax(worst_res, __longlong_as_double((long long)res));
-            worst_viol = fmax(worst_viol, __longlong_as_double((long long)vb));
+            if (tid == 0) {
+                worst[0] = umax(worst[0], res);
+                worst[1] = umax(worst[1], vb);
+            }
         }
         for (int i = tid; i < a.n; i += BD) a.out[(size_t)i * (size_t)a.ld_out + (size_t)p] = any_accepted ? xs[i] : 0.0;
         if (a.A_out)
             for (int i = tid; i < a.n; i += BD) a.A_out[(size_t)i * (size_t)a.ld_state + (size_t)p] = As[i];
         __syncthreads();
     }
+#undef ACHR_CHAIN_ID
 
     __syncthreads();
     if (tid == 0) {
@@ -1006,8 +1014,8 @@ __global__ void __launch_bounds__(BD, (BD <= 384 ? 2 : 1)) achr_chain_kernel(con
         for (int q = 0; q < 6; ++q)
             if (cnt[slots[q]]) atomicAdd(c + slots[q], cnt[slots[q]]);
         if (*exact_count) atomicAdd(c + CNT_EXACT, (unsigned long long)*exact_count);
-        if (worst_res > 0.0) atomicMax(c + CNT_MAXRES_BITS, (unsigned long long)__double_as_longlong(worst_res));
-        if (worst_viol > 0.0) atomicMax(c + CNT_MAXVIOL_BITS, (unsigned long long)__double_as_longlong(worst_viol));
+        if (worst[0]) atomicMax(c + CNT_MAXRES_BITS, worst[0]);
+        if (worst[1]) atomicMax(c + CNT_MAXVIOL_BITS, worst[1]);
         if (failed) atomicOr(c + CNT_ERROR, ERR_TMA_TIMEOUT);
     }
 }
