@@ -379,6 +379,12 @@ __device__ __forceinline__ void residual_form_reproject(const ChainArgs &a, doub
     }
 }
 
+// Bytes of one staged warmup column (the leading dimension is even, so a
+// multiple of 16).
+__device__ __forceinline__ unsigned column_bytes(const ChainArgs &a) {
+    return (unsigned)(sizeof(double) * (size_t)a.ldw);
+}
+
 }  // namespace
 
 constexpr int kTbl = 64;  // steps per refill of the step table
@@ -426,9 +432,6 @@ __global__ void __launch_bounds__(BD, (BD <= 384 ? 2 : 1)) achr_chain_kernel(con
     for (int k = 0; k < EPT; ++k) ws[tid + k * BD] = 0.0;
     __syncthreads();
 
-    const unsigned col_bytes = (unsigned)(sizeof(double) * (size_t)a.ldw);
-    const float dtol_hi = a.dtol_hi, dtol_lo = a.dtol_lo, berr = a.bound_err;
-    const float utol32 = a.utol32, mmt32 = a.mmt32;
     const bool hr = a.hit_and_run != 0;  // directions are the staged columns themselves (no centre)
     const bool merged = a.merged_ab != 0 && !a.exact_ratio;  // ratio-test brackets formed in phase A
     const float uthr_max = a.uthr_max;
@@ -457,20 +460,19 @@ __global__ void __launch_bounds__(BD, (BD <= 384 ? 2 : 1)) achr_chain_kernel(con
         }
         int buf_col = -1;
         bool inflight = false, any_accepted = a.x_in != nullptr, stuck = false;
-        const int s_end = a.step0 + a.T;
         // The reference checks when the step count is a multiple of the period
         // (ACHRCuda.cu:325); a period of INT_MAX stands for "never".
         int chk = a.check_period == 0x7fffffff ? 1 : a.step0 % a.check_period;
         int tbase = a.step0 - kTbl;
 
-        for (int s = a.step0; s < s_end && !stuck && !failed; ++s) {
+        for (int s = a.step0; s < (a.step0 + a.T) && !stuck && !failed; ++s) {
             if (s - tbase >= kTbl) {
                 // refill the step table: entry e holds step tbase + e
                 tbase = s;
                 __syncthreads();
                 for (int e = tid; e < kTbl; e += BD) {
                     const int st = s + e;
-                    if (st < s_end) {
+                    if (st < (a.step0 + a.T)) {
                         const Philox4 pd = step_draw(a.seed, ACHR_CHAIN_ID, (uint32_t)st, 0u);
                         StepEntry en;
                         en.U = step_uniform(pd);
@@ -507,8 +509,8 @@ __global__ void __launch_bounds__(BD, (BD <= 384 ? 2 : 1)) achr_chain_kernel(con
                     }
                     if (tid == 0) {
                         fence_proxy_async_smem();
-                        mbar_arrive_expect_tx(bar, col_bytes);
-                        tma_load_1d(ws, a.warmup + (size_t)r * (size_t)a.ldw, col_bytes, bar);
+                        mbar_arrive_expect_tx(bar, column_bytes(a));
+                        tma_load_1d(ws, a.warmup + (size_t)r * (size_t)a.ldw, column_bytes(a), bar);
                     }
                     inflight = true;
                     buf_col = r;
@@ -563,13 +565,13 @@ __global__ void __launch_bounds__(BD, (BD <= 384 ? 2 : 1)) achr_chain_kernel(con
                 float my_lh = INFINITY, my_ll = INFINITY;  // this thread's smallest bracket lower ends
                 int fl = 0;
                 if (merged) {
-                    const float uthr_lo_p = utol32 * admax * kProvDn;
+                    const float uthr_lo_p = a.utol32 * admax * kProvDn;
 #pragma unroll
                     for (int k = 0; k < EPT; ++k) {
                         const int i = tid + k * BD;
                         float lo_h, lo_l;
-                        bracket(xs[i], dreg[k], __ldg(a.bnd + i), berr, dtol_hi, dtol_lo, uthr_max, uthr_lo_p, lo_h,
-                                lo_l, uh, ul, fl);
+                        bracket(xs[i], dreg[k], __ldg(a.bnd + i), a.bound_err, a.dtol_hi, a.dtol_lo, uthr_max,
+                                uthr_lo_p, lo_h, lo_l, uh, ul, fl);
                         my_lh = fminf(my_lh, lo_h);
                         my_ll = fminf(my_ll, lo_l);
                     }
@@ -611,7 +613,7 @@ __global__ void __launch_bounds__(BD, (BD <= 384 ? 2 : 1)) achr_chain_kernel(con
                 const float norm32 = sqrtf(ss);
 
                 // Prefetch the next step's warmup column while this one is tested.
-                if (s + 1 < s_end) {
+                if (s + 1 < (a.step0 + a.T)) {
                     const int rn =
                         (s + 1 - tbase < kTbl)
                             ? (int)tbl[s + 1 - tbase].idx
@@ -619,8 +621,8 @@ __global__ void __launch_bounds__(BD, (BD <= 384 ? 2 : 1)) achr_chain_kernel(con
                     if (rn != buf_col && rn >= 0 && rn < a.W) {
                         if (tid == 0) {
                             fence_proxy_async_smem();
-                            mbar_arrive_expect_tx(bar, col_bytes);
-                            tma_load_1d(ws, a.warmup + (size_t)rn * (size_t)a.ldw, col_bytes, bar);
+                            mbar_arrive_expect_tx(bar, column_bytes(a));
+                            tma_load_1d(ws, a.warmup + (size_t)rn * (size_t)a.ldw, column_bytes(a), bar);
                         }
                         inflight = true;
                         buf_col = rn;
@@ -632,7 +634,7 @@ __global__ void __launch_bounds__(BD, (BD <= 384 ? 2 : 1)) achr_chain_kernel(con
                 }
 
                 // Phase B1: FP32 brackets (reference ratio test ACHRCuda.cu:266-281)
-                const float uthr = utol32 * norm32;
+                const float uthr = a.utol32 * norm32;
                 const float uthr_hi = uthr * kNormUp, uthr_lo = uthr * kNormDn;
                 if (merged && uthr_hi <= uthr_max) {
                     fl = 0;  // the merged brackets stand; their flags are not used
@@ -649,8 +651,8 @@ __global__ void __launch_bounds__(BD, (BD <= 384 ? 2 : 1)) achr_chain_kernel(con
                         for (int k = 0; k < EPT; ++k) {
                             const int i = tid + k * BD;
                             float lo_h, lo_l;
-                            bracket(xs[i], dreg[k], __ldg(a.bnd + i), berr, dtol_hi, dtol_lo, uthr_hi, uthr_lo, lo_h,
-                                    lo_l, uh, ul, fl);
+                            bracket(xs[i], dreg[k], __ldg(a.bnd + i), a.bound_err, a.dtol_hi, a.dtol_lo, uthr_hi,
+                                    uthr_lo, lo_h, lo_l, uh, ul, fl);
                             my_lh = fminf(my_lh, lo_h);  // NaN (not a candidate) is ignored, -inf (undecided) wins
                             my_ll = fminf(my_ll, lo_l);
                         }
@@ -720,8 +722,8 @@ __global__ void __launch_bounds__(BD, (BD <= 384 ? 2 : 1)) achr_chain_kernel(con
                             const int i = tid + k * BD;
                             float lo_h, lo_l, uh2 = INFINITY, ul2 = INFINITY;  // minima already known
                             int fl2 = 0;
-                            bracket(xs[i], dreg[k], __ldg(a.bnd + i), berr, dtol_hi, dtol_lo, uthr_hi, uthr_lo, lo_h,
-                                    lo_l, uh2, ul2, fl2);
+                            bracket(xs[i], dreg[k], __ldg(a.bnd + i), a.bound_err, a.dtol_hi, a.dtol_lo, uthr_hi,
+                                    uthr_lo, lo_h, lo_l, uh2, ul2, fl2);
                             mh |= (lo_h <= uh ? 1u : 0u) << k;
                             ml |= (lo_l <= ul ? 1u : 0u) << k;
                             mam |= (lo_h == -INFINITY ? 1u : 0u) << k;
@@ -795,7 +797,7 @@ __global__ void __launch_bounds__(BD, (BD <= 384 ? 2 : 1)) achr_chain_kernel(con
                     const float qh32 = f64_to_f32_rz(qh), ql32 = f64_to_f32_rz(ql);
                     const float th_lo = qh32 * norm32 * kNormDn, th_hi = qh32 * kAdUp * norm32 * kNormUp;
                     const float tl_lo = ql32 * norm32 * kNormDn, tl_hi = ql32 * kAdUp * norm32 * kNormUp;
-                    const float tol_lo = mmt32 * kDn, tol_hi = mmt32 * kUp;
+                    const float tol_lo = a.mmt32 * kDn, tol_hi = a.mmt32 * kUp;
                     const bool big = th_lo >= tol_hi || tl_lo >= tol_hi;
                     const bool small = th_hi < tol_lo && tl_hi < tol_lo;
                     if (big) {
@@ -836,7 +838,7 @@ __global__ void __launch_bounds__(BD, (BD <= 384 ? 2 : 1)) achr_chain_kernel(con
                         const int i = tid + k * BD;
                         const double xn = fma(sstep, dreg[k], xs[i]);
                         xs[i] = xn;
-                        if (!surely_inside(f64_to_f32_rz(xn), __ldg(a.bnd + i), berr)) edge |= 1u << k;
+                        if (!surely_inside(f64_to_f32_rz(xn), __ldg(a.bnd + i), a.bound_err)) edge |= 1u << k;
                     }
                     for (; edge; edge &= edge - 1) {
                         const int i = tid + (__ffs(edge) - 1) * BD;
@@ -849,7 +851,7 @@ __global__ void __launch_bounds__(BD, (BD <= 384 ? 2 : 1)) achr_chain_kernel(con
                         const int i = tid + k * BD;
                         const double xn = fma(sstep, dreg[k], xs[i]);
                         xs[i] = xn;
-                        if (surely_inside(f64_to_f32_rz(xn), __ldg(a.bnd + i), berr)) As[i] += xn;
+                        if (surely_inside(f64_to_f32_rz(xn), __ldg(a.bnd + i), a.bound_err)) As[i] += xn;
                         else edge |= 1u << k;
                     }
                     for (; edge; edge &= edge - 1) {
@@ -908,8 +910,8 @@ __global__ void __launch_bounds__(BD, (BD <= 384 ? 2 : 1)) achr_chain_kernel(con
                         if (buf_col >= 0) {
                             if (tid == 0) {
                                 fence_proxy_async_smem();
-                                mbar_arrive_expect_tx(bar, col_bytes);
-                                tma_load_1d(ws, a.warmup + (size_t)buf_col * (size_t)a.ldw, col_bytes, bar);
+                                mbar_arrive_expect_tx(bar, column_bytes(a));
+                                tma_load_1d(ws, a.warmup + (size_t)buf_col * (size_t)a.ldw, column_bytes(a), bar);
                             }
                             inflight = true;
                         }
@@ -919,7 +921,7 @@ __global__ void __launch_bounds__(BD, (BD <= 384 ? 2 : 1)) achr_chain_kernel(con
                     for (int k = 0; k < EPT; ++k) {
                         const int i = tid + k * BD;
                         const double xv = xs[i];
-                        if (surely_inside(f64_to_f32_rz(xv), __ldg(a.bnd + i), berr)) {
+                        if (surely_inside(f64_to_f32_rz(xv), __ldg(a.bnd + i), a.bound_err)) {
                             if (!hr) As[i] += xv;
                         } else {
                             edge |= 1u << k;
