@@ -1,4 +1,7 @@
-// Chain-kernel instantiations with 320 and 384 threads per chain (two CTAs per SM).
+// Chain-kernel instantiations between the power-of-two lengths: 320 x 12 and
+// 384 x 10 (3840 elements, two CTAs per SM), 512 x 12 (6144) and 512 x 15
+// (7680, one CTA per SM), so that models of 4097-7680 reactions do not pad to
+// 8192.
 #include "achr_chain_kernel.cuh"
 
 namespace achr {
@@ -7,6 +10,8 @@ cudaError_t launch_chain_cfg_mid(int bd, int ept, const ChainArgs &a, cudaStream
     switch (bd * 100 + ept) {
         case 320 * 100 + 12: return launch_cfg<320, 12>(a, s, max_ctas, per_sm);
         case 384 * 100 + 10: return launch_cfg<384, 10>(a, s, max_ctas, per_sm);
+        case 512 * 100 + 12: return launch_cfg<512, 12>(a, s, max_ctas, per_sm);
+        case 512 * 100 + 15: return launch_cfg<512, 15>(a, s, max_ctas, per_sm);
         default: return cudaErrorInvalidValue;
     }
 }

@@ -23,12 +23,14 @@ struct Cfg {
 // 320 x 12 and 384 x 10 (3840 elements) put 20 or 24 warps on an SM with two
 // chains each, against 16 for 256 x 16, at the cost of fewer registers per
 // thread; 384 x 10 is the default up to 3840 reactions (2.04e7 against 1.95e7
-// chain-steps/s for 256 x 16 on a 2766 x 3742 model).
+// chain-steps/s for 256 x 16 on a 2766 x 3742 model).  512 x 12 and 512 x 15
+// cut the padding of 4097-7680 reactions (a 7440-reaction model pads to 7680,
+// not 8192: 3 % of the FP64 work on padding instead of 10 %).
 const Cfg kLadder[] = {
     {32, 4, true},    {64, 4, true},    {32, 8, false},   {128, 4, true},  {64, 8, false},
     {128, 8, true},   {256, 4, false},  {256, 8, true},   {128, 16, false}, {512, 4, false},
     {320, 12, false}, {384, 10, true},  {256, 16, true},  {512, 8, false},  {128, 32, false},
-    {512, 16, true},  {512, 32, true},
+    {512, 12, true},  {512, 15, true},  {512, 16, true},  {512, 32, true},
 };
 
 const Cfg *find_cfg(int n, int threads_per_chain) {
@@ -84,7 +86,8 @@ cudaError_t launch_chains(const ChainArgs &a, int threads_per_chain, cudaStream_
     if (!c || c->bd * c->ept > a.np) return cudaErrorInvalidValue;
     if (a.P <= 0 && !per_sm) return cudaSuccess;
     if (c->bd <= 128) return launch_chain_cfg_small(c->bd, c->ept, a, stream, max_ctas, per_sm);
-    if (c->bd == 320 || c->bd == 384) return launch_chain_cfg_mid(c->bd, c->ept, a, stream, max_ctas, per_sm);
+    if (c->bd == 320 || c->bd == 384 || (c->bd == 512 && (c->ept == 12 || c->ept == 15)))
+        return launch_chain_cfg_mid(c->bd, c->ept, a, stream, max_ctas, per_sm);
     return launch_chain_cfg_large(c->bd, c->ept, a, stream, max_ctas, per_sm);
 }
 

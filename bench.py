@@ -467,7 +467,7 @@ def run_batch(args):
             warm = synth.interior_chord_warmup(S, lb, ub, 2 * n, seed=spec.seed, null_space=gpu_null_space,
                                                interior=interiors[k])
             np.savez(cache, warm=warm)
-        s = pkg.Sampler(pkg.HostModel(n, spec.n_mets, row, col, val, lb, ub), warm)
+        s = pkg.Sampler(pkg.HostModel(n, spec.n_mets, row, col, val, lb, ub), warm, bracket_pass=args.bracket_pass)
         s.autotune()
         samplers.append(s)
         outs.append(torch.empty((n, int(P[k])), dtype=torch.float64, device="cuda"))
@@ -756,7 +756,7 @@ def run_large(args):
     P = args.large_chains
     period, Tr = 100, args.large_steps
     n = spec.n_rxns
-    smp = pkg.Sampler(model, warm, check_period=0)
+    smp = pkg.Sampler(model, warm, check_period=0, **sampler_options(args))
     tpc = smp.autotune()
     x = torch.zeros((n, P), dtype=torch.float64, device="cuda")
     a = torch.zeros_like(x)
@@ -790,7 +790,7 @@ def run_large(args):
     torch.cuda.empty_cache()
     # Plain ACHR on the same chains: per-chain residual check every 10 steps,
     # FP64 reprojection of a chain when it fires (reference semantics).
-    plain = pkg.Sampler(model, warm)
+    plain = pkg.Sampler(model, warm, **sampler_options(args))
     plain.autotune()
     out = torch.empty((n, P), dtype=torch.float64, device="cuda")
     plain.sample_device(P, 20, out.data_ptr(), P, stream=stream, seed=args.seed)
