@@ -435,6 +435,12 @@ __global__ void __launch_bounds__(BD, (BD <= 384 ? 2 : 1)) achr_chain_kernel(con
     const bool hr = a.hit_and_run != 0;  // directions are the staged columns themselves (no centre)
     const bool merged = a.merged_ab != 0 && !a.exact_ratio;  // ratio-test brackets formed in phase A
     const float uthr_max = a.uthr_max;
+    // A warp whose 32 elements of the last slot (k = EPT - 1) all lie in the
+    // padding (i >= n) skips that slot: its coordinates stay 0 and its d is 0,
+    // so the FP64 operations on it would change nothing.
+    const bool tail_live = warp * 32 + (EPT - 1) * BD < a.n;
+// (Not for 32 elements per thread, where the branches cost more registers than they save.)
+#define ACHR_PAD_SLOT(k) (EPT < 32 && (k) == EPT - 1 && !tail_live)
     unsigned phase = 0, it = 0;
     bool failed = false;
 
@@ -536,6 +542,10 @@ __global__ void __launch_bounds__(BD, (BD <= 384 ? 2 : 1)) achr_chain_kernel(con
 #pragma unroll
                     for (int k = 0; k < EPT; ++k) {
                         const int i = tid + k * BD;
+                        if (ACHR_PAD_SLOT(k)) {
+                            dreg[k] = 0.0;
+                            continue;
+                        }
                         const double dk = ws[i];
                         dreg[k] = dk;
                         const float d32 = f64_to_f32_rz(dk);
@@ -547,6 +557,10 @@ __global__ void __launch_bounds__(BD, (BD <= 384 ? 2 : 1)) achr_chain_kernel(con
 #pragma unroll
                     for (int k = 0; k < EPT; ++k) {
                         const int i = tid + k * BD;
+                        if (ACHR_PAD_SLOT(k)) {
+                            dreg[k] = 0.0;
+                            continue;
+                        }
                         const double dk = fma(As[i], ninv, ws[i]);
                         dreg[k] = dk;
                         const float d32 = f64_to_f32_rz(dk);
@@ -569,6 +583,7 @@ __global__ void __launch_bounds__(BD, (BD <= 384 ? 2 : 1)) achr_chain_kernel(con
 #pragma unroll
                     for (int k = 0; k < EPT; ++k) {
                         const int i = tid + k * BD;
+                        if (ACHR_PAD_SLOT(k)) continue;  // padding: never a candidate
                         float lo_h, lo_l;
                         bracket(xs[i], dreg[k], __ldg(a.bnd + i), a.bound_err, a.dtol_hi, a.dtol_lo, uthr_max,
                                 uthr_lo_p, lo_h, lo_l, uh, ul, fl);
@@ -650,6 +665,7 @@ __global__ void __launch_bounds__(BD, (BD <= 384 ? 2 : 1)) achr_chain_kernel(con
 #pragma unroll
                         for (int k = 0; k < EPT; ++k) {
                             const int i = tid + k * BD;
+                            if (ACHR_PAD_SLOT(k)) continue;
                             float lo_h, lo_l;
                             bracket(xs[i], dreg[k], __ldg(a.bnd + i), a.bound_err, a.dtol_hi, a.dtol_lo, uthr_hi,
                                     uthr_lo, lo_h, lo_l, uh, ul, fl);
@@ -720,6 +736,7 @@ __global__ void __launch_bounds__(BD, (BD <= 384 ? 2 : 1)) achr_chain_kernel(con
 #pragma unroll
                         for (int k = 0; k < EPT; ++k) {
                             const int i = tid + k * BD;
+                            if (ACHR_PAD_SLOT(k)) continue;
                             float lo_h, lo_l, uh2 = INFINITY, ul2 = INFINITY;  // minima already known
                             int fl2 = 0;
                             bracket(xs[i], dreg[k], __ldg(a.bnd + i), a.bound_err, a.dtol_hi, a.dtol_lo, uthr_hi,
@@ -836,6 +853,7 @@ __global__ void __launch_bounds__(BD, (BD <= 384 ? 2 : 1)) achr_chain_kernel(con
 #pragma unroll
                     for (int k = 0; k < EPT; ++k) {
                         const int i = tid + k * BD;
+                        if (ACHR_PAD_SLOT(k)) continue;
                         const double xn = fma(sstep, dreg[k], xs[i]);
                         xs[i] = xn;
                         if (!surely_inside(f64_to_f32_rz(xn), __ldg(a.bnd + i), a.bound_err)) edge |= 1u << k;
@@ -849,6 +867,7 @@ __global__ void __launch_bounds__(BD, (BD <= 384 ? 2 : 1)) achr_chain_kernel(con
 #pragma unroll
                     for (int k = 0; k < EPT; ++k) {
                         const int i = tid + k * BD;
+                        if (ACHR_PAD_SLOT(k)) continue;
                         const double xn = fma(sstep, dreg[k], xs[i]);
                         xs[i] = xn;
                         if (surely_inside(f64_to_f32_rz(xn), __ldg(a.bnd + i), a.bound_err)) As[i] += xn;
@@ -864,6 +883,7 @@ __global__ void __launch_bounds__(BD, (BD <= 384 ? 2 : 1)) achr_chain_kernel(con
 #pragma unroll
                     for (int k = 0; k < EPT; ++k) {
                         const int i = tid + k * BD;
+                        if (ACHR_PAD_SLOT(k)) continue;
                         xs[i] = fma(sstep, dreg[k], xs[i]);
                     }
                     __syncthreads();
@@ -920,6 +940,7 @@ __global__ void __launch_bounds__(BD, (BD <= 384 ? 2 : 1)) achr_chain_kernel(con
 #pragma unroll
                     for (int k = 0; k < EPT; ++k) {
                         const int i = tid + k * BD;
+                        if (ACHR_PAD_SLOT(k)) continue;
                         const double xv = xs[i];
                         if (surely_inside(f64_to_f32_rz(xv), __ldg(a.bnd + i), a.bound_err)) {
                             if (!hr) As[i] += xv;
@@ -1008,6 +1029,7 @@ __global__ void __launch_bounds__(BD, (BD <= 384 ? 2 : 1)) achr_chain_kernel(con
         __syncthreads();
     }
 #undef ACHR_CHAIN_ID
+#undef ACHR_PAD_SLOT
 
     __syncthreads();
     if (tid == 0) {
