@@ -393,7 +393,9 @@ def run_profile_case(args):
     pkg.lib()
     import importlib
     synth = importlib.import_module("achr_gb300.synthetic")
-    spec, model, S, warm, _, _ = build_inputs(args.workload, pkg, synth)
+    # the same warmup construction as the workload's own bench run (the large one uses the GPU null space)
+    ns = gpu_null_space_fn(pkg) if args.workload == "large" else None
+    spec, model, S, warm, _, _ = build_inputs(args.workload, pkg, synth, null_space=ns)
     P, T = args.profile_case
     smp = pkg.Sampler(model, warm, **sampler_options(args))
     out = torch.empty((spec.n_rxns, P), dtype=torch.float64, device="cuda")
@@ -923,14 +925,14 @@ def main():
         return run_gemm(args)
     if args.learned:
         return run_learned(args)
+    if args.profile_case:
+        return run_profile_case(args)
     if args.workload == "large" and args.impl == "gb300" and not args.ess:
         return run_large(args)
     if args.ess:
         return run_ess(args)
     if args.workload == "batch64":
         return run_batch(args)
-    if args.profile_case:
-        return run_profile_case(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_gpu(args)
