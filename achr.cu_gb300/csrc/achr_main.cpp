@@ -13,6 +13,8 @@
 //   --check-period N    residual check every N steps (default 10, ACHRCuda.cu:325; 0 = never)
 //   --reproject nnt|residual  per-chain reprojection as N (N^T x) or through the residual
 //                       (default: chosen by model size)
+//   --bracket-pass merged|separate  ratio-test brackets in the direction pass (default) or in a
+//                       pass of their own; the points are the same
 //   --writer-threads N  host threads formatting File<ii>
 //   --report path.json  write sampling statistics
 #include <cuda_runtime.h>
@@ -53,7 +55,8 @@ int main(int argc, char **argv) {
         std::fprintf(stderr,
                      "usage: %s model.mps warmuppoints.csv nFiles nPoints nSteps [--seed S] [--mode reference|feasible]"
                      " [--null sts|svd] [--centre cuda|matlab] [--threads-per-chain N] [--check-period N]"
-                     " [--reproject nnt|residual] [--writer-threads N] [--report file.json]\n",
+                     " [--reproject nnt|residual] [--bracket-pass merged|separate] [--writer-threads N]"
+                     " [--report file.json]\n",
                      argv[0]);
         return 2;
     }
@@ -101,6 +104,11 @@ int main(int argc, char **argv) {
             if (m == "nnt") opt.reproject_form = 1;
             else if (m == "residual") opt.reproject_form = 2;
             else return std::fprintf(stderr, "ACHRCuda: bad --reproject\n"), 2;
+        } else if (f == "--bracket-pass") {
+            std::string m = need();
+            if (m == "merged") opt.bracket_pass = 0;
+            else if (m == "separate") opt.bracket_pass = 1;
+            else return std::fprintf(stderr, "ACHRCuda: bad --bracket-pass\n"), 2;
         } else if (f == "--writer-threads") {
             if (!parse_int(need(), v)) return std::fprintf(stderr, "ACHRCuda: bad --writer-threads\n"), 2;
             writer_threads = (int)v;

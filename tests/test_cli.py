@@ -32,7 +32,7 @@ def test_cli_bad_numbers(native, pkg, tmp_path):
 
 
 @pytest.mark.parametrize("flags", [["--reproject", "fast"], ["--check-period", "-1"], ["--mode", "x"],
-                                   ["--seed"], ["--bogus", "1"]])
+                                   ["--bracket-pass", "both"], ["--seed"], ["--bogus", "1"]])
 def test_cli_bad_flags(native, pkg, tmp_path, flags):
     r = _run(pkg, [GOLDEN / "small.mps", GOLDEN / "small_warmup.csv", 1, 2, 2, *flags], tmp_path)
     assert r.returncode == 2
