@@ -85,6 +85,7 @@ class DeviceModel(C.Structure):
         ("n_rxns", C.c_int32), ("n_mets", C.c_int32), ("n_warmup", C.c_int32), ("null_dim", C.c_int32),
         ("ld_warmup", C.c_int64), ("warmup", C.c_void_p), ("lb", C.c_void_p), ("ub", C.c_void_p),
         ("row_ptr", C.c_void_p), ("col_idx", C.c_void_p), ("val", C.c_void_p), ("N", C.c_void_p),
+        ("nnz", C.c_int64),
     ]
 
 

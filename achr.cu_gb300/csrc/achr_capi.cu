@@ -55,17 +55,8 @@ void f32_bound(double v, float &f, float &err) {
     err = ef;
 }
 
-float f32_up(double v) {
-    float f = (float)v;
-    if ((double)f < v) f = std::nextafter(f, INFINITY);
-    return f;
-}
-
-float f32_down(double v) {
-    float f = (float)v;
-    if ((double)f > v) f = std::nextafter(f, -INFINITY);
-    return f;
-}
+using achr::f32_down;
+using achr::f32_up;
 
 // Writes the global nanosecond timer (used to time each model's branch of a
 // batched graph).
@@ -604,19 +595,7 @@ achr_status achr_sample_device(achr_ctx *ctx, uint64_t seed, uint64_t chain_offs
 
 namespace {
 
-// Upper bound of the FP32 candidacy threshold u_tol ||d|| (times its margin)
-// for the brackets formed before the block norm is known, from a bound on
-// ||d||; without a finite bound the brackets keep their own pass.
-void set_merged_bound(ChainArgs &a, double u_tol, double dnorm_max) {
-    const double t = u_tol * dnorm_max * 1.01;
-    if (std::isfinite(t) && t > 0.0 && t < 1e30) {
-        a.uthr_max = f32_up(t);
-        a.merged_ab = 1;
-    } else {
-        a.uthr_max = 0.0f;
-        a.merged_ab = 0;
-    }
-}
+using achr::set_merged_bound;
 
 ChainArgs chain_args(const achr_ctx *ctx, uint64_t seed, uint64_t chain_offset, int32_t n_points, int32_t n_steps,
                      double *d_points_out, int64_t ld_out) {

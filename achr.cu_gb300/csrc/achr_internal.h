@@ -3,6 +3,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <cmath>
+
 namespace achr {
 
 // Counters kept in device memory while a sampling launch runs.
@@ -77,6 +79,32 @@ struct ChainArgs {
     unsigned long long wait_ns;    // limit of the wait for a staged column (0: the default, 2 s)
     int wait_never;                // 1: that wait is on a barrier nothing completes (tests the timeout)
 };
+
+// FP32 rounding of a double toward +inf / -inf (host side).
+inline float f32_up(double v) {
+    float f = (float)v;
+    if ((double)f < v) f = nextafterf(f, __builtin_huge_valf());
+    return f;
+}
+inline float f32_down(double v) {
+    float f = (float)v;
+    if ((double)f > v) f = nextafterf(f, -__builtin_huge_valf());
+    return f;
+}
+
+// Upper bound of the FP32 candidacy threshold u_tol ||d|| (times its margin)
+// for the ratio-test brackets formed before the block norm is known, from a
+// bound on ||d||; without a finite bound the brackets keep their own pass.
+inline void set_merged_bound(ChainArgs &a, double u_tol, double dnorm_max) {
+    const double t = u_tol * dnorm_max * 1.01;
+    if (t == t && t > 0.0 && t < 1e30) {
+        a.uthr_max = f32_up(t);
+        a.merged_ab = 1;
+    } else {
+        a.uthr_max = 0.0f;
+        a.merged_ab = 0;
+    }
+}
 
 // Launch the persistent chain kernel; threads_per_chain = 0 picks the default
 // configuration for n.  max_ctas > 0 caps the grid; per_sm (if non-NULL)

@@ -22,7 +22,13 @@
 //               lanes 32 (w mod 4) .. +31), store FP32 rows of C and hand the
 //               accumulator back, while the MMAs of the next tile run.
 // Every mbarrier wait is bounded (2 s); on expiry the kernel records an error
-// bit, skips the rest of its work and still frees its tensor memory.
+// bit and skips the rest of its work.  Before the CTA leaves, the producer
+// waits for every TMA load it issued to land (so no copy writes into shared
+// memory the CTA no longer owns) and the MMA thread waits for every MMA it
+// issued to complete before tensor memory is freed.  An MMA is issued only
+// after its operands have landed, so it depends on nothing but the tensor
+// pipe and always completes; that wait is repeated, bounded each time, until
+// it does.
 #include <cuda.h>
 #include <cudaTypedefs.h>
 #include <cuda_runtime.h>
@@ -229,6 +235,15 @@ __global__ void __launch_bounds__(kThreads, 1)
                     tma_2d(sa + kABytes, mb, kx, n0, bar_full + 8 * s);
                 }
             }
+            // Drain: the last load armed on each stage (use it/kStages - 1 or the
+            // round below it) must have landed before shared memory is released.
+            // Each stage is at most one phase ahead of its last arming, so the
+            // parity names that phase unambiguously.
+            for (int j = (it > kStages ? it - kStages : 0); j < it; ++j) {
+                const int s = j % kStages;
+                const unsigned round = (unsigned)(j / kStages);
+                if (!bar_wait(bar_full + 8 * s, round & 1u)) ok = false;
+            }
         }
     } else if (warp == 1) {
         if (lane == 0) {
@@ -260,8 +275,10 @@ __global__ void __launch_bounds__(kThreads, 1)
                 if (ok) tc_commit(bar_accf + 8 * b);
             }
             // Before tensor memory is freed: every MMA issued above has completed.
+            // (Their operands had landed when they were issued, so they finish;
+            // the bounded wait is repeated rather than abandoned.)
             tc_commit(bar_done);
-            if (!bar_wait(bar_done, 0)) ok = false;
+            for (int tries = 0; tries < 8 && !bar_wait(bar_done, 0); ++tries) ok = false;
         }
         __syncwarp();
     } else {

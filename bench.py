@@ -76,6 +76,9 @@ def parse_args():
     ap.add_argument("--large-chains", type=int, default=262_144, help="chains of the large workload")
     ap.add_argument("--large-steps", type=int, default=200, help="timed steps of the large workload")
     ap.add_argument("--threads-per-chain", type=int, default=0, help="chain-kernel block size (0: by model size)")
+    ap.add_argument("--warmup-form", choices=["percent_f", "exact"], default="exact",
+                    help="warmup points as the reference's %%f CSV holds them, or exact FP64 chord points")
+    ap.add_argument("--chains", type=int, default=0, help="override the workload's chain count (0: its own)")
     ap.add_argument("--bracket-pass", type=int, choices=[0, 1], default=0,
                     help="0: ratio-test brackets formed with the direction; 1: a separate pass")
     ap.add_argument("--profile-case", type=int, nargs=2, metavar=("CHAINS", "STEPS"),
@@ -123,12 +126,24 @@ def gpu_null_space_fn(pkg):
     return null_space
 
 
-def build_inputs(workload, pkg, synth, null_space=None):
+def percent_f(pkg, warm, tag):
+    """The warmup matrix as the reference reads it: written with "%f" (one line per reaction, as
+    VFWarmup/createWarmupPtsGLPK.c:289-297 writes it) and read back (ACHRcu/ACHRCuda.cu:675-689),
+    through the library's own writer and reader."""
+    path = Path("/tmp") / f"achr_bench_{tag}_warmup.csv"
+    pkg.write_points_csv(path, warm)
+    out = pkg.read_warmup_csv(path, warm.shape[0])
+    path.unlink()
+    return out
+
+
+def build_inputs(workload, pkg, synth, null_space=None, warmup_form="exact"):
     """Model arrays, dense S and warmup points (numpy; identical for both arms).
-    Cached under /tmp so the two arms of one run share the set-up work."""
+    Cached under /tmp so the two arms of one run share the set-up work.  warmup_form
+    "percent_f" rounds the points to six decimals as the reference's CSV holds them."""
     spec_name, P, T = WORKLOADS[workload]
     spec = getattr(synth, spec_name)
-    cache = Path("/tmp") / f"achr_bench_{workload}_{spec.seed}_v2.npz"
+    cache = Path("/tmp") / f"achr_bench_{workload}_{spec.seed}_{warmup_form}_v2.npz"
     row, col, val, lb, ub = synth.make_model(spec)
     S = synth.dense(spec.n_mets, spec.n_rxns, row, col, val)
     W = 2 * spec.n_rxns
@@ -136,6 +151,8 @@ def build_inputs(workload, pkg, synth, null_space=None):
         warm = np.load(cache)["warm"]
     else:
         warm = synth.interior_chord_warmup(S, lb, ub, W, seed=spec.seed + 17, null_space=null_space)
+        if warmup_form == "percent_f":
+            warm = percent_f(pkg, warm, f"{workload}_{spec.seed}")
         np.savez(cache, warm=warm)
     model = pkg.HostModel(spec.n_rxns, spec.n_mets, row, col, val, lb, ub)
     return spec, model, S, warm, P, T
@@ -233,7 +250,9 @@ def run_reference(args):
     import importlib
     synth = importlib.import_module("achr_gb300.synthetic")
     oracle.build()
-    spec, model, S, warm, P, T = build_inputs(args.workload, pkg, synth)
+    spec, model, S, warm, P, T = build_inputs(args.workload, pkg, synth, warmup_form=args.warmup_form)
+    if args.chains:
+        P = args.chains
     N = oracle_null_space(S)
     threads = os.cpu_count() or 1
     prob = oracle.Problem(model, warm, N)
@@ -254,7 +273,8 @@ def run_reference(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": f"{args.workload}: {spec.n_mets}x{spec.n_rxns} synthetic model, W={warm.shape[1]}, "
-                               f"{P} chains x {T} steps (CPU step = {Pstep} chains x {T} steps)",
+                               f"{P} chains x {T} steps (CPU step = {Pstep} chains x {T} steps), "
+                               f"warmups {args.warmup_form}",
                    "parallelism": f"openmp{threads}"},
         "cpu_baseline": {"value": value, "unit": METRIC, "cores": threads, "kind": "port",
                          "sample": f"{Pstep} chains x {T} steps per step, {args.steps} steps"},
@@ -282,7 +302,9 @@ def run_gpu(args):
     pkg = ge.load_package()
     pkg.lib()
     synth = importlib.import_module("achr_gb300.synthetic")
-    spec, model, S, warm, P, T = build_inputs(args.workload, pkg, synth)
+    spec, model, S, warm, P, T = build_inputs(args.workload, pkg, synth, warmup_form=args.warmup_form)
+    if args.chains:
+        P = args.chains
     n = spec.n_rxns
     sharding = importlib.import_module("achr_gb300.sharding")
     chain_base, _ = sharding.chain_block(rank, world, P)  # weak scaling: every rank runs its own P chains
@@ -362,7 +384,7 @@ def run_gpu(args):
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": f"{args.workload}: {spec.n_mets}x{spec.n_rxns} synthetic model, W={warm.shape[1]}, "
-                               f"{P} chains x {T} steps per GPU, mode=reference",
+                               f"{P} chains x {T} steps per GPU, mode=reference, warmups {args.warmup_form}",
                    "global_batch": world * P, "seq_len": T, "parallelism": f"chains sharded over {world} GPU(s)",
                    "l2": "inputs exceed L2 (warmup matrix 224 MB > 129 MB); no flush",
                    "options": sampler_options(args)},
@@ -395,7 +417,7 @@ def run_profile_case(args):
     synth = importlib.import_module("achr_gb300.synthetic")
     # the same warmup construction as the workload's own bench run (the large one uses the GPU null space)
     ns = gpu_null_space_fn(pkg) if args.workload == "large" else None
-    spec, model, S, warm, _, _ = build_inputs(args.workload, pkg, synth, null_space=ns)
+    spec, model, S, warm, _, _ = build_inputs(args.workload, pkg, synth, null_space=ns, warmup_form=args.warmup_form)
     P, T = args.profile_case
     smp = pkg.Sampler(model, warm, **sampler_options(args))
     out = torch.empty((spec.n_rxns, P), dtype=torch.float64, device="cuda")

@@ -339,8 +339,8 @@ achr_status achr_sample_batch(achr_ctx *const *ctxs, int32_t n_models, const int
 /* ---- Sampling without any allocation ---- */
 
 /* Largest model (reactions) achr_sample_noalloc accepts: its working data sits
- * in a fixed array of about 40 bytes per reaction (321 KB) that every GPU
- * loading the library keeps until the process exits. */
+ * in a fixed array of about 40 bytes per reaction plus 1.3 KB (322 KB) that
+ * every GPU loading the library keeps until the process exits. */
 #define ACHR_NOALLOC_MAX_RXNS 8192
 
 /* A model already resident in device memory (all pointers are device pointers). */
@@ -352,25 +352,33 @@ typedef struct {
     int64_t ld_warmup;        /* leading dimension of warmup in doubles: even and >= n_rxns */
     const double *warmup;     /* ld_warmup x W, column j = warmup point j; 16-byte aligned */
     const double *lb, *ub;    /* n bounds */
-    const int32_t *row_ptr;   /* CSR of S: m + 1 offsets */
+    const int32_t *row_ptr;   /* CSR of S: m + 1 offsets, row_ptr[0] = 0, row_ptr[m] = nnz */
     const int32_t *col_idx;   /* nnz column indices in [0, n) */
     const double *val;        /* nnz coefficients */
     const double *N;          /* n x d column-major null-space basis */
+    int64_t nnz;              /* entries of col_idx and val */
 } achr_device_model;
 
 /* No counterpart in the reference (which allocates all its buffers itself).
- * Same sampling as achr_sample_device, for callers that may not allocate GPU
- * memory (code inside another framework's memory pool or a pre-sized arena,
- * or a repeated path that must not add allocations): inputs and the n x P
- * output (leading dimension ld_out) are the caller's device buffers, and the
- * library calls no cudaMalloc, cudaFree or allocating library routine.  Its
- * working data lives in one fixed device array shared by all calls; the first
- * call on each device looks up that array's address (make it before any
- * stream capture); calls whose GPU work overlaps race on it and must be
- * serialised.  Models above ACHR_NOALLOC_MAX_RXNS reactions are rejected with
- * ACHR_ERR_UNSUPPORTED.  The null space is the caller's (as with
- * achr_set_null_space); in ACHR_MODE_FEASIBLE only the final projection of
- * emitted points is applied.  Synchronises the stream; stats->kernel_ms is 0. */
+ * The points of achr_sample_device (same seed, chains and options), for
+ * callers that may not allocate GPU memory (code inside another framework's
+ * memory pool or a pre-sized arena, or a repeated path that must not add
+ * allocations): inputs and the n x P output (leading dimension ld_out) are the
+ * caller's device buffers, and the library calls no cudaMalloc, cudaFree or
+ * allocating library routine.  Its working data lives in one fixed device
+ * array shared by all calls; the first call on each device looks up that
+ * array's address (make it before any stream capture); calls whose GPU work
+ * overlaps race on it and must be serialised.  Models above
+ * ACHR_NOALLOC_MAX_RXNS reactions are rejected with ACHR_ERR_UNSUPPORTED.
+ * The model is checked on the device before sampling (CSR offsets and column
+ * indices, finite coefficients and warmup values, lb <= ub); a bad model gives
+ * ACHR_ERR_INVALID.  What differs from a context: the null space is the
+ * caller's (as with achr_set_null_space); the residual check reads the
+ * caller's CSR rather than a sliced-ELL copy (same sums); reprojection is
+ * N (N^T x) in FP64 (reproject_form 2 gives ACHR_ERR_UNSUPPORTED); in
+ * ACHR_MODE_FEASIBLE only the final projection of emitted points is applied
+ * (the warmup points are used as given).  Synchronises the stream and reports
+ * an expired column wait as ACHR_ERR_TIMEOUT; stats->kernel_ms is 0. */
 achr_status achr_sample_noalloc(const achr_device_model *model, const achr_options *opt, uint64_t seed,
                                 uint64_t chain_offset, int32_t n_points, int32_t n_steps, double *d_points_out,
                                 int64_t ld_out, void *stream, achr_stats *stats);

@@ -56,6 +56,21 @@ def small_model(pkg, golden):
     return pkg.HostModel(int(g["n_rxns"]), int(g["n_mets"]), g["row"], g["col"], g["val"], g["lb"], g["ub"])
 
 
+@pytest.fixture(scope="session")
+def putida_files(tmp_path_factory):
+    """The reference's P_Putida model and its 2n %f warmup CSV, unpacked from tests/golden/."""
+    import gzip
+    import shutil
+
+    d = tmp_path_factory.mktemp("putida")
+    out = []
+    for name in ("P_Putida.mps", "putida_warmup.csv"):
+        with gzip.open(GOLDEN / (name + ".gz"), "rb") as f, open(d / name, "wb") as g:
+            shutil.copyfileobj(f, g)
+        out.append(d / name)
+    return tuple(out)
+
+
 def dense_S(model):
     S = np.zeros((model.n_mets, model.n_rxns))
     np.add.at(S, (np.asarray(model.row), np.asarray(model.col)), np.asarray(model.val))

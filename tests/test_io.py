@@ -10,10 +10,6 @@ import pytest
 
 from conftest import GOLDEN
 
-# The reference checkout's own fixture model; the test runs only where
-# ACHR_REFERENCE_DIR names a checkout of the reference project.
-_REF_DIR = os.environ.get("ACHR_REFERENCE_DIR")
-REF_PUTIDA = Path(_REF_DIR, "VFWarmup", "lib", "P_Putida.mps") if _REF_DIR else Path("")
 
 
 def test_read_golden_mps(native, pkg, golden):
@@ -63,15 +59,29 @@ def _independent_mps_parse(path):
     return len(rows), len(cols), trip, np.array([lb[c] for c in order]), np.array([ub[c] for c in order])
 
 
-@pytest.mark.skipif(not REF_PUTIDA.is_file(), reason="ACHR_REFERENCE_DIR does not name a reference checkout")
-def test_read_reference_putida_model(native, pkg):
+def test_read_reference_putida_model(native, pkg, putida_files):
     """The reference's own fixture model (VFWarmup/lib/P_Putida.mps): 911 rows, 1060 columns."""
-    m = pkg.read_mps(REF_PUTIDA)
-    nm, nr, trip, lb, ub = _independent_mps_parse(REF_PUTIDA)
+    mps, _ = putida_files
+    m = pkg.read_mps(mps)
+    nm, nr, trip, lb, ub = _independent_mps_parse(mps)
     assert (m.n_mets, m.n_rxns) == (nm, nr) == (911, 1060)
     assert np.array_equal(m.lb, lb) and np.array_equal(m.ub, ub)
     got = sorted(zip(m.row.tolist(), m.col.tolist(), m.val.tolist()))
     assert got == sorted(trip)
+    assert (m.val != np.round(m.val)).sum() > 0  # non-integer coefficients
+
+
+def test_read_reference_form_warmup_csv(native, pkg, putida_files):
+    """2n %f-rounded warmup points of P_Putida: every value has at most six decimals, and the
+    rounding leaves S w non-zero, as the reference's input does."""
+    mps, csv = putida_files
+    m = pkg.read_mps(mps)
+    w = pkg.read_warmup_csv(csv, m.n_rxns)
+    assert w.shape == (1060, 2120)
+    assert np.abs(np.round(w * 1e6) - w * 1e6).max() < 1e-3 * np.abs(w).max()
+    assert (w >= m.lb[:, None]).all() and (w <= m.ub[:, None]).all()
+    r = np.abs(m.dense() @ w).max()
+    assert 1e-9 < r < 1e-4
 
 
 def _write(tmp_path, name, text):
