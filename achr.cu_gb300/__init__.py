@@ -65,6 +65,7 @@ class Options(C.Structure):
         ("reproject_form", C.c_int32),
         ("residual_tol", C.c_double), ("max_min_tol", C.c_double), ("u_tol", C.c_double), ("d_tol", C.c_double),
         ("feasibility_tol", C.c_double), ("wait_limit_ns", C.c_int32), ("bracket_pass", C.c_int32),
+        ("reprojection_passes", C.c_int32),
     ]
 
 
@@ -73,6 +74,7 @@ class Stats(C.Structure):
         ("accepted", C.c_int64), ("rejected", C.c_int64), ("checks", C.c_int64), ("reprojections", C.c_int64),
         ("stuck_chains", C.c_int64), ("exact_evals", C.c_int64), ("final_projections", C.c_int64),
         ("max_residual", C.c_double), ("max_bound_violation", C.c_double), ("kernel_ms", C.c_double),
+        ("segments", C.c_int64),
     ]
 
     def as_dict(self) -> dict:

@@ -78,6 +78,28 @@ __global__ void centre_kernel(int n, int W, int ldw, const double *__restrict__ 
     A0[i] = (double)(W + centre_offset) * c;
 }
 
+// Largest |S w|_inf over the warmup points (one block per point, a thread per
+// row of the device CSR), as the bits of a non-negative double, maxed into *out_bits.
+__global__ void warmup_residual_kernel(int m, int ldw, const double *__restrict__ warmup, const int *__restrict__ rp,
+                                       const int *__restrict__ ci, const double *__restrict__ rv,
+                                       unsigned long long *out_bits) {
+    __shared__ unsigned long long part[32];
+    const double *w = warmup + (size_t)blockIdx.x * (size_t)ldw;
+    unsigned long long mx = 0;
+    for (int i = threadIdx.x; i < m; i += blockDim.x) {
+        double acc = 0.0;
+        for (int q = rp[i]; q < rp[i + 1]; ++q) acc = fma(rv[q], w[ci[q]], acc);
+        mx = max(mx, (unsigned long long)__double_as_longlong(acc) & 0x7FFFFFFFFFFFFFFFull);
+    }
+    for (int o = 16; o; o >>= 1) mx = max(mx, (unsigned long long)__shfl_xor_sync(0xffffffffu, mx, o));
+    if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = mx;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int k = 1; k < (int)(blockDim.x >> 5); ++k) mx = max(mx, part[k]);
+        atomicMax(out_bits, mx);
+    }
+}
+
 // Largest column norm of an n x K column-major matrix (one block per column),
 // as the bits of a non-negative double, maxed into *out_bits.
 __global__ void col_norm_max_kernel(int n, long long ld, const double *__restrict__ M,
@@ -133,7 +155,9 @@ achr_status validate_options(const achr_options &o) {
         return fail(ACHR_ERR_INVALID, "unknown null_space method");
     if (o.check_period < 0) return fail(ACHR_ERR_INVALID, "check_period must be >= 0 (0: no in-loop checks)");
     if (o.max_attempts <= 0) return fail(ACHR_ERR_INVALID, "max_attempts must be positive");
-    if (o.reproject_form < 0 || o.reproject_form > 2) return fail(ACHR_ERR_INVALID, "reproject_form must be 0, 1 or 2");
+    if (o.reproject_form < 0 || o.reproject_form > 3) return fail(ACHR_ERR_INVALID, "reproject_form must be 0..3");
+    if (o.reprojection_passes < 0 || o.reprojection_passes > 8)
+        return fail(ACHR_ERR_INVALID, "reprojection_passes must be 0..8");
     if (o.centre_offset != 0 && o.centre_offset != 1) return fail(ACHR_ERR_INVALID, "centre_offset must be 0 or 1");
     if (o.bracket_pass != 0 && o.bracket_pass != 1) return fail(ACHR_ERR_INVALID, "bracket_pass must be 0 or 1");
     if (o.threads_per_chain != 0 && o.threads_per_chain != 32 && o.threads_per_chain != 64 &&
@@ -292,6 +316,20 @@ achr_status prepare_warmup_and_centre(achr_ctx *ctx) {
     centre_kernel<<<(n + 127) / 128, 128>>>(n, W, ctx->ldw, ctx->warmup.p, ctx->opt.centre_offset, ctx->c0.p,
                                             ctx->A0.p);
     ACHR_CUDA_TRY(cudaGetLastError());
+    // The residual the warmup points carry as they will be sampled (a %f CSV
+    // leaves about 1e-6; it decides where reprojections run, see defer_selected).
+    ctx->warmup_residual = 0.0;
+    if (ctx->m > 0) {
+        DevBuf<unsigned long long> rb;
+        ACHR_CUDA_TRY(rb.alloc(1));
+        ACHR_CUDA_TRY(cudaMemset(rb.p, 0, sizeof(unsigned long long)));
+        warmup_residual_kernel<<<W, 128>>>(ctx->m, ctx->ldw, ctx->warmup.p, ctx->rowptr.p, ctx->colidx.p, ctx->val.p,
+                                           rb.p);
+        ACHR_CUDA_TRY(cudaGetLastError());
+        unsigned long long bits = 0;
+        ACHR_CUDA_TRY(cudaMemcpy(&bits, rb.p, sizeof bits, cudaMemcpyDeviceToHost));
+        std::memcpy(&ctx->warmup_residual, &bits, sizeof(double));
+    }
     ACHR_CUDA_TRY(cudaDeviceSynchronize());
     return ACHR_OK;
 }
@@ -304,6 +342,8 @@ achr_status read_counters(achr_ctx *ctx, achr_stats *stats, float ms) {
     ACHR_CUDA_TRY(cudaMemcpy(c, ctx->counters.p, sizeof(c), cudaMemcpyDeviceToHost));
     if (c[achr::CNT_ERROR] & achr::ERR_TMA_TIMEOUT)
         return fail(ACHR_ERR_TIMEOUT, "a warmup-column copy did not complete within its wait limit");
+    if (c[achr::CNT_ERROR] & achr::ERR_TC_TIMEOUT)
+        return fail(ACHR_ERR_TIMEOUT, "a tensor-core pipeline wait of the batched reprojection expired");
     if (stats) {
         stats->accepted = (int64_t)c[achr::CNT_ACCEPTED];
         stats->rejected = (int64_t)c[achr::CNT_REJECTED];
@@ -318,6 +358,7 @@ achr_status read_counters(achr_ctx *ctx, achr_stats *stats, float ms) {
         stats->max_residual = r;
         stats->max_bound_violation = v;
         stats->kernel_ms = ms;
+        stats->segments = 0;
     }
     return ACHR_OK;
 }
@@ -575,11 +616,23 @@ achr_status achr_sample_device(achr_ctx *ctx, uint64_t seed, uint64_t chain_offs
         ACHR_CUDA_TRY(cudaEventCreate(&e1));
         ACHR_CUDA_TRY(cudaEventRecord(e0, s));
     }
-    cudaError_t e = achr::launch_chains(a, ctx->opt.threads_per_chain, s);
-    if (e != cudaSuccess) {
+    // Reprojections either inside the chain kernel, or deferred to a batched
+    // tensor-core pass between segmented launches (achr_defer.cu).
+    const bool deferred = achr::defer_selected(ctx) && n_points > 0 && n_steps > 0;
+    if (ctx->opt.reproject_form == 3 && !deferred && n_points > 0 && n_steps > 0 && ctx->opt.check_period > 0 &&
+        ctx->m > 0) {
         if (e0) cudaEventDestroy(e0);
         if (e1) cudaEventDestroy(e1);
-        return cuda_fail(e, "chain kernel launch");
+        return fail(ACHR_ERR_UNSUPPORTED, "deferred reprojection needs n_mets <= the chain kernel's padded length");
+    }
+    cudaError_t e = cudaSuccess;
+    achr_status dst = ACHR_OK;
+    if (deferred) dst = achr::defer_sample(ctx, a, ctx->opt.threads_per_chain, s);
+    else e = achr::launch_chains(a, ctx->opt.threads_per_chain, s);
+    if (e != cudaSuccess || dst != ACHR_OK) {
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+        return dst != ACHR_OK ? dst : cuda_fail(e, "chain kernel launch");
     }
     if (!stats) return ACHR_OK;
     ACHR_CUDA_TRY(cudaEventRecord(e1, s));
@@ -588,7 +641,9 @@ achr_status achr_sample_device(achr_ctx *ctx, uint64_t seed, uint64_t chain_offs
     cudaEventElapsedTime(&ms, e0, e1);
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    return read_counters(ctx, stats, ms);
+    achr_status rst = read_counters(ctx, stats, ms);
+    if (rst == ACHR_OK) stats->segments = deferred ? ctx->last_segments : 0;
+    return rst;
 }
 
 }  // extern "C"
@@ -770,6 +825,7 @@ achr_status achr_sample(achr_ctx *ctx, uint64_t seed, uint64_t chain_offset, int
 
 void achr_destroy(achr_ctx *ctx) {
     if (!ctx) return;
+    achr::defer_free(ctx->defer);
     achr::reproj_free(ctx->reproj);
     delete ctx;
 }

@@ -319,6 +319,52 @@ __device__ __forceinline__ unsigned long long residual_max_bits(const ChainArgs 
     return mx;
 }
 
+// The same row sums as residual_max_bits (same rows, same order of terms, so
+// the same maximum), each stored to rr[row] (device row order) for the
+// batched reprojection of segmented sampling.
+template <int BD>
+__device__ __forceinline__ unsigned long long residual_rows(const ChainArgs &a, const double *xs, double *rr, int tid) {
+    unsigned long long mx = 0;
+    if (a.sell_off) {
+        const int lane = tid & 31;
+        for (int g = tid >> 5; g < a.sell_groups; g += BD / 32) {
+            const int base = __ldg(a.sell_off + g);
+            const int len = (__ldg(a.sell_off + g + 1) - base) >> 5;
+            double acc = 0.0;
+#pragma unroll 4
+            for (int t = 0; t < len; ++t) {
+                const int q = base + (t << 5) + lane;
+                acc = fma(__ldg(a.sell_val + q), xs[__ldg(a.sell_col + q)], acc);
+            }
+            mx = umax(mx, abs_bits(acc));
+            const int row = (g << 5) + lane;
+            if (row < a.m) rr[row] = acc;
+        }
+    } else {
+        for (int row = tid; row < a.m; row += BD) {
+            double acc = 0.0;
+            const int q1 = __ldg(a.row_ptr + row + 1);
+            for (int q = __ldg(a.row_ptr + row); q < q1; ++q) acc = fma(__ldg(a.val + q), xs[__ldg(a.col_idx + q)], acc);
+            mx = umax(mx, abs_bits(acc));
+            rr[row] = acc;
+        }
+    }
+    return mx;
+}
+
+// BF16 bits of v rounded to nearest (hi) and of the remainder v - hi (lo).
+__device__ __forceinline__ void split_bf16_bits(double v, unsigned short &hi, unsigned short &lo) {
+    const float f = __double2float_rn(v);
+    unsigned u = __float_as_uint(f);
+    // round-to-nearest-even of the FP32 value to its upper 16 bits (finite values)
+    const unsigned hu = (u + 0x7FFFu + ((u >> 16) & 1u)) & 0xFFFF0000u;
+    hi = (unsigned short)(hu >> 16);
+    const float rem = __double2float_rn(v - (double)__uint_as_float(hu));
+    unsigned r = __float_as_uint(rem);
+    const unsigned ru = (r + 0x7FFFu + ((r >> 16) & 1u)) & 0xFFFF0000u;
+    lo = (unsigned short)(ru >> 16);
+}
+
 // x <- x - S^T z, z = (S S^T)^+ S x: the reference's N (N^T x) written through
 // the residual (equal in exact arithmetic).  S x is summed in FP64 over the
 // same rows as the check and kept as FP32 hi + lo pairs in rr (m entries of
@@ -448,7 +494,17 @@ __global__ void __launch_bounds__(BD, (BD <= 384 ? 2 : 1)) achr_chain_kernel(con
     // parameters where they are used rather than held in registers.)
     for (int p = blockIdx.x; p < a.P && !failed; p = (int)min((long long)p + gridDim.x, (long long)a.P)) {
 #define ACHR_CHAIN_ID (a.chain_offset + (unsigned long long)p)
-        if (a.x_in) {  // resume: the chain's point and centre accumulator after step0 steps
+        // Segmented sampling: the chain's state bits from the earlier launches.
+        const unsigned sflags = a.seg ? a.seg_flags[p] : 0u;
+        if (sflags & SEG_STARTED) {
+#pragma unroll
+            for (int k = 0; k < EPT; ++k) {
+                const int i = tid + k * BD;
+                const bool real = i < a.n;
+                xs[i] = real ? a.seg_x[(size_t)p * (size_t)a.ld_seg + (size_t)i] : 0.0;
+                As[i] = real ? a.seg_A[(size_t)p * (size_t)a.ld_seg + (size_t)i] : 0.0;
+            }
+        } else if (a.x_in) {  // resume: the chain's point and centre accumulator after step0 steps
 #pragma unroll
             for (int k = 0; k < EPT; ++k) {
                 const int i = tid + k * BD;
@@ -465,13 +521,39 @@ __global__ void __launch_bounds__(BD, (BD <= 384 ? 2 : 1)) achr_chain_kernel(con
             }
         }
         int buf_col = -1;
-        bool inflight = false, any_accepted = a.x_in != nullptr, stuck = false;
+        bool inflight = false, any_accepted = a.x_in != nullptr || (sflags & SEG_ACCEPTED), stuck = false;
+        bool seg_pending = false;  // this launch ended the chain after a check step's update
+        const bool was_stuck = (sflags & SEG_STUCK) != 0;
+        if (was_stuck) stuck = true;  // stopped in an earlier launch: no more steps
+        if (sflags & SEG_PENDING) {
+            // Finish the check step the previous launch ended on (the batched
+            // pass has reprojected the point if its residual was above the
+            // tolerance): clip, then add the point to the centre accumulator.
+            unsigned edge = 0;
+#pragma unroll
+            for (int k = 0; k < EPT; ++k) {
+                const int i = tid + k * BD;
+                if (ACHR_PAD_SLOT(k)) continue;
+                const double xv = xs[i];
+                if (surely_inside(f64_to_f32_rz(xv), __ldg(a.bnd + i), a.bound_err)) {
+                    if (!hr) As[i] += xv;
+                } else {
+                    edge |= 1u << k;
+                }
+            }
+            for (; edge; edge &= edge - 1) {
+                const int i = tid + (__ffs(edge) - 1) * BD;
+                const double xc = clip_exact(xs[i], ld_lbub(a.lbub + i));
+                xs[i] = xc;
+                if (!hr) As[i] += xc;
+            }
+        }
         // The reference checks when the step count is a multiple of the period
         // (ACHRCuda.cu:325); a period of INT_MAX stands for "never".
         int chk = a.check_period == 0x7fffffff ? 1 : a.step0 % a.check_period;
         int tbase = a.step0 - kTbl;
 
-        for (int s = a.step0; s < (a.step0 + a.T) && !stuck && !failed; ++s) {
+        for (int s = a.step0; s < (a.step0 + a.T) && !stuck && !failed && !seg_pending; ++s) {
             if (s - tbase >= kTbl) {
                 // refill the step table: entry e holds step tbase + e
                 tbase = s;
@@ -879,6 +961,61 @@ __global__ void __launch_bounds__(BD, (BD <= 384 ? 2 : 1)) achr_chain_kernel(con
                         xs[i] = xc;
                         As[i] += xc;
                     }
+                } else if (a.seg) {
+                    // Segmented sampling: the check ends this launch for the chain.
+#pragma unroll
+                    for (int k = 0; k < EPT; ++k) {
+                        const int i = tid + k * BD;
+                        if (ACHR_PAD_SLOT(k)) continue;
+                        xs[i] = fma(sstep, dreg[k], xs[i]);
+                    }
+                    if (inflight) {  // (the launch ends here, so nothing was prefetched; kept for safety)
+                        if (!mbar_wait_bounded(bar, phase)) failed = true;
+                        phase ^= 1u;
+                        inflight = false;
+                    }
+                    __syncthreads();  // every x update visible; the staging buffer is free
+                    if (tid == 0) ++cnt[CNT_CHECKS];
+                    double *rr = ws;  // S x, m doubles (m <= BD * EPT for segmented launches)
+                    unsigned long long mx = residual_rows<BD>(a, xs, rr, tid);
+                    mx = warp_max_u64(mx);
+                    if (lane == 0) rs->max4[warp] = mx;
+                    __syncthreads();
+                    mx = 0;
+#pragma unroll
+                    for (int w = 0; w < NW; ++w) mx = umax(mx, rs->max4[w]);
+                    const bool reproject = mx > (unsigned long long)__double_as_longlong(a.residual_tol);
+                    if (reproject) {
+                        if (tid == 0) {
+                            ++cnt[CNT_REPROJ];
+                            if (*a.seg_any == 0ull) atomicOr(a.seg_any, 1ull);
+                        }
+                        unsigned short *rh = a.seg_Rh + (size_t)p * (size_t)a.kpad;
+                        unsigned short *rl = a.seg_Rl + (size_t)p * (size_t)a.kpad;
+                        for (int q = tid; q < a.m; q += BD) {
+                            unsigned short h, l;
+                            split_bf16_bits(rr[q], h, l);
+                            const int row = __ldg(a.row_orig + q);
+                            rh[row] = h;
+                            rl[row] = l;
+                        }
+                    }
+#pragma unroll
+                    for (int k = 0; k < EPT; ++k) {
+                        const int i = tid + k * BD;
+                        if (i < a.n) {
+                            a.seg_x[(size_t)p * (size_t)a.ld_seg + (size_t)i] = xs[i];
+                            a.seg_A[(size_t)p * (size_t)a.ld_seg + (size_t)i] = As[i];
+                        }
+                    }
+                    if (tid == 0) {
+                        a.seg_flags[p] = SEG_STARTED | SEG_ACCEPTED | SEG_PENDING | (reproject ? SEG_REPROJ : 0u);
+                        ++cnt[CNT_ACCEPTED];
+                    }
+                    __syncthreads();  // the residual rows in ws are read before the next chain's column lands
+                    any_accepted = true;
+                    seg_pending = true;
+                    break;
                 } else {
 #pragma unroll
                     for (int k = 0; k < EPT; ++k) {
@@ -965,10 +1102,27 @@ __global__ void __launch_bounds__(BD, (BD <= 384 ? 2 : 1)) achr_chain_kernel(con
             phase ^= 1u;
             inflight = false;
         }
-        if (stuck && tid == 0) ++cnt[CNT_STUCK];
+        if (stuck && !was_stuck && tid == 0) ++cnt[CNT_STUCK];
         if (__syncthreads_or(failed ? 1 : 0)) {
             failed = true;
             break;
+        }
+        if (a.seg && !seg_pending && !a.seg_final) {
+            // A segmented launch that is not the run's last: keep the state for the next one.
+#pragma unroll
+            for (int k = 0; k < EPT; ++k) {
+                const int i = tid + k * BD;
+                if (i < a.n) {
+                    a.seg_x[(size_t)p * (size_t)a.ld_seg + (size_t)i] = xs[i];
+                    a.seg_A[(size_t)p * (size_t)a.ld_seg + (size_t)i] = As[i];
+                }
+            }
+            if (tid == 0)
+                a.seg_flags[p] = SEG_STARTED | (any_accepted ? SEG_ACCEPTED : 0u) | (stuck ? SEG_STUCK : 0u);
+        }
+        if (a.seg && (seg_pending || !a.seg_final)) {
+            __syncthreads();
+            continue;  // the point is emitted by the run's last launch
         }
 
         // Emitted point: residual / bound diagnostics and, on request, the final

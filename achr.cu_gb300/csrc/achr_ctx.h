@@ -1,5 +1,6 @@
 // Sampler context shared by the C-ABI translation units.
 #pragma once
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <vector>
@@ -39,8 +40,23 @@ struct DevBuf {
     }
 };
 
-struct ReprojState;
+// Operator of the batched reprojection x <- x - S^T B S x, B = (S S^T)^+
+// (achr_reproject.cu), built on first use.
+struct ReprojState {
+    int m = 0, n = 0, kpad = 0, rank = 0, device = 0;
+    double lam_max = 0.0, lam_min = 0.0;
+    DevBuf<__nv_bfloat16> Bh, Bl;  // m x kpad row-major: (S S^T)^+ split into hi + lo
+    DevBuf<int> rp, ci, cp, ri;    // CSR and CSC of S (original row order)
+    DevBuf<double> rv, cv;
+    DevBuf<__nv_bfloat16> Rh, Rl;  // chunk x kpad: residuals of a chunk of chains, hi + lo
+    DevBuf<float> Z;               // m x chunk: B r for the chunk
+    int chunk_cap = 0;
+    DevBuf<unsigned long long> flags;  // [1] max|Sx| bits after, [2] device error bits, [8 + r * chunks + c] round r, chunk c
+};
 void reproj_free(ReprojState *r);  // achr_reproject.cu
+
+struct DeferState;
+void defer_free(DeferState *d);  // achr_defer.cu
 
 }  // namespace achr
 
@@ -49,6 +65,14 @@ namespace achr {
 // (S S^T)^+ in FP32, rows and columns in the device row order, into ctx->pinv32
 // (achr_reproject.cu; builds the batched-reprojection operator on the way).
 achr_status build_pinv32(achr_ctx *ctx);
+// The batched-reprojection operator of the context, built on first use.
+achr_status ensure_reproj(achr_ctx *ctx);
+// Segmented sampling with the per-chain reprojections deferred to a batched
+// pass (achr_defer.cu): runs the launch described by `a` (a.P chains of a.T
+// steps from step 0) on `stream`.
+achr_status defer_sample(achr_ctx *ctx, const ChainArgs &a, int threads_per_chain, cudaStream_t stream);
+// Whether sampling with these options takes the deferred path.
+bool defer_selected(const achr_ctx *ctx);
 }  // namespace achr
 
 struct achr_ctx {
@@ -77,6 +101,9 @@ struct achr_ctx {
     achr::DevBuf<float> pinv32;            // (S S^T)^+ in FP32, device row order, m x m (empty: not built)
     achr::DevBuf<unsigned long long> counters;
     achr::ReprojState *reproj = nullptr;  // batched reprojection operator, built on first use
+    achr::DeferState *defer = nullptr;    // buffers of segmented sampling, built on first use
+    double warmup_residual = 0.0;         // max |S w|_inf over the warmup points (as sampled)
+    long long last_segments = 0;          // chain-kernel launches of the last deferred-reprojection run
     achr::DevBuf<double> dirs;   // hit-and-run direction pool, n x n_dirs (leading dimension ldw)
     int n_dirs = 0;              // 0: ACHR directions (warmup point minus centre)
     achr::DevBuf<double> zeros;  // np zeros: the (unused) centre accumulator of hit-and-run chains

@@ -1,0 +1,253 @@
+// Segmented sampling: the reference's per-chain reprojection deferred to one
+// batched pass over all chains on the tensor cores.
+//
+// The reference checks every 10th step whether max|S x| exceeds 1e-9 and, if
+// so, reprojects that chain, x <- N (N^T x), with two FP64 GEMVs before it
+// clips the point and updates the centre (ACHRcu/ACHRCuda.cu:325-350,
+// reprojectPoint(2) :208-230).  With warmup points read from the %f CSV the
+// reference's warmup generator writes (VFWarmup/createWarmupPtsGLPK.c:292),
+// |S w| is about 1e-6 and nearly every check reprojects; per chain that is
+// 4 n d FP64 operations, about a hundred times the FP64 work of the step
+// itself at 2766 x 3742 on GB300's FP64 pipe.
+//
+// Here every chain runs to its next check step in one launch of the chain
+// kernel (segmented mode, achr_chain_kernel.cuh), which ends each chain right
+// after the check step's x <- x + t u and leaves, for every chain whose
+// residual exceeds the tolerance, S x (FP64, split into BF16 hi + lo) in a
+// chain-major block R.  The batched pass then applies the same orthogonal
+// projector to all of those chains at once,
+//
+//     x <- x - S^T z,   z = B (S x),   B = (S S^T)^+,
+//
+// z for every chain as one tensor-core GEMM Z = R B^T (three BF16 split
+// products, FP32 accumulation, achr_tc_gemm.cu) and the update S^T z in FP64.
+// The low-precision product only ever sees the residual, and the update lies
+// in the row space of S, so the null-space part of x is untouched and each
+// further pass multiplies what is left of the row-space part by about 1e-3:
+// two passes leave the point within ~1e-12 of the FP64 projection.  The next
+// launch of the chain kernel clips each point and adds it to its centre
+// accumulator before the chain's next step, the order the reference uses.
+// The decisions (which chains reproject) are the chain kernel's own FP64
+// residual, identical to the check it makes when it reprojects in place.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <new>
+#include <string>
+
+#include "achr_ctx.h"
+
+extern "C" void achr_io_set_error(const char *msg);
+
+namespace achr {
+
+struct DeferState {
+    int cap = 0;             // chains the buffers hold
+    long long ld = 0;        // leading dimension of the chain-major state (n rounded up to even)
+    int ldz = 0;             // leading dimension of Z (m rounded up to a multiple of 4)
+    int kpad = 0;            // K of the GEMM: m rounded up to a multiple of 64
+    DevBuf<double> x, A;     // cap x ld: points and centre accumulators between launches
+    DevBuf<unsigned> flags;  // cap: SEG_* bits
+    DevBuf<unsigned short> Rh, Rl;  // cap x kpad BF16 bits: S x of the chains that reproject
+    DevBuf<float> Z;         // cap x ldz: B (S x)
+    DevBuf<int> row_orig;    // m: device row order of S -> the model's row order
+    DevBuf<unsigned long long> any;  // one word per launch: some chain needs the batched pass
+    int any_cap = 0;
+};
+
+void defer_free(DeferState *d) { delete d; }
+
+namespace {
+
+constexpr int kDeferChunk = 131072;  // chains per sweep through the segments (bounds the buffers)
+constexpr int kCorrThreads = 256;
+
+achr_status set_err(achr_status st, const std::string &msg) {
+    achr_io_set_error(msg.c_str());
+    return st;
+}
+
+#define DEFER_TRY(expr)                                                                                        \
+    do {                                                                                                       \
+        cudaError_t e_ = (expr);                                                                               \
+        if (e_ != cudaSuccess) return set_err(ACHR_ERR_CUDA, std::string(#expr) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+// x <- x - S^T z for every chain flagged SEG_REPROJ (one CTA per chain at a
+// time, chain-major rows so every load and store is coalesced; z from the
+// GEMM's row of that chain), then, for the next pass, S x again (FP64) as
+// BF16 hi/lo into R.  S is read in the model's row order (CSC for S^T z, CSR
+// for S x), matching the rows of B.
+__global__ void __launch_bounds__(kCorrThreads)
+    defer_correct_kernel(int n, int m, int kpad, int P, double *__restrict__ X, long long ldx,
+                         const unsigned *__restrict__ flags, const float *__restrict__ Z, long long ldz,
+                         const int *__restrict__ cp, const int *__restrict__ ri, const double *__restrict__ cv,
+                         const int *__restrict__ rp, const int *__restrict__ ci, const double *__restrict__ rv,
+                         __nv_bfloat16 *__restrict__ Rh, __nv_bfloat16 *__restrict__ Rl, int want_residual) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    double *xsm = reinterpret_cast<double *>(smem_raw);
+    float *zs = reinterpret_cast<float *>(xsm + ldx);
+    const int tid = threadIdx.x;
+    for (int p = blockIdx.x; p < P; p += gridDim.x) {
+        if (!(flags[p] & SEG_REPROJ)) continue;  // uniform over the block
+        const float *zp = Z + (size_t)p * (size_t)ldz;
+        for (int i = tid; i < m; i += kCorrThreads) zs[i] = zp[i];
+        __syncthreads();
+        double *xp = X + (size_t)p * (size_t)ldx;
+        for (int j = tid; j < n; j += kCorrThreads) {
+            double dl = 0.0;
+            const int q1 = __ldg(cp + j + 1);
+            for (int q = __ldg(cp + j); q < q1; ++q) dl = fma(__ldg(cv + q), (double)zs[__ldg(ri + q)], dl);
+            const double xv = xp[j] - dl;
+            xp[j] = xv;
+            xsm[j] = xv;
+        }
+        __syncthreads();
+        if (want_residual) {
+            __nv_bfloat16 *rh = Rh + (size_t)p * (size_t)kpad, *rl = Rl + (size_t)p * (size_t)kpad;
+            for (int i = tid; i < m; i += kCorrThreads) {
+                double acc = 0.0;
+                const int q1 = __ldg(rp + i + 1);
+                for (int q = __ldg(rp + i); q < q1; ++q) acc = fma(__ldg(rv + q), xsm[__ldg(ci + q)], acc);
+                const __nv_bfloat16 hi = __double2bfloat16(acc);
+                rh[i] = hi;
+                rl[i] = __double2bfloat16(acc - (double)__bfloat162float(hi));
+            }
+        }
+        __syncthreads();
+    }
+}
+
+achr_status ensure_defer(achr_ctx *ctx, int chains, int segments) {
+    DeferState *D = ctx->defer;
+    if (!D) {
+        D = new (std::nothrow) DeferState();
+        if (!D) return set_err(ACHR_ERR_NOMEM, "allocation failed");
+        ctx->defer = D;
+        const ReprojState &R = *ctx->reproj;
+        D->kpad = R.kpad;
+        D->ld = (ctx->n + 1) & ~1;
+        D->ldz = (ctx->m + 3) & ~3;
+        DEFER_TRY(D->row_orig.upload(ctx->h_row_order.data(), ctx->h_row_order.size()));
+    }
+    if (D->cap < chains) {
+        D->cap = 0;
+        const size_t c = (size_t)chains;
+        DEFER_TRY(D->x.alloc(c * (size_t)D->ld));
+        DEFER_TRY(D->A.alloc(c * (size_t)D->ld));
+        DEFER_TRY(D->flags.alloc(c));
+        DEFER_TRY(D->Rh.alloc(c * (size_t)D->kpad));
+        DEFER_TRY(D->Rl.alloc(c * (size_t)D->kpad));
+        // the K padding of R (rows m..kpad) is never written and must be zero
+        DEFER_TRY(cudaMemset(D->Rh.p, 0, sizeof(unsigned short) * c * (size_t)D->kpad));
+        DEFER_TRY(cudaMemset(D->Rl.p, 0, sizeof(unsigned short) * c * (size_t)D->kpad));
+        DEFER_TRY(D->Z.alloc(c * (size_t)D->ldz));
+        D->cap = chains;
+    }
+    if (D->any_cap < segments) {
+        D->any_cap = 0;
+        DEFER_TRY(D->any.alloc((size_t)segments));
+        D->any_cap = segments;
+    }
+    return ACHR_OK;
+}
+
+}  // namespace
+
+bool defer_selected(const achr_ctx *ctx) {
+    const achr_options &o = ctx->opt;
+    if (o.check_period <= 0 || ctx->m <= 0) return false;
+    const int np = chain_padded_length(ctx->n, o.threads_per_chain);
+    if (np == 0 || ctx->m > np) return false;  // S x is staged in the chain kernel's column buffer
+    if (o.reproject_form == 3) return true;
+    if (o.reproject_form != 0 || ctx->n_dirs > 0) return false;
+    return ctx->warmup_residual > o.residual_tol / 8.0 && (double)ctx->n * (double)ctx->d >= 2.5e5;
+}
+
+achr_status defer_sample(achr_ctx *ctx, const ChainArgs &a_in, int threads_per_chain, cudaStream_t s) {
+    achr_status st = ensure_reproj(ctx);
+    if (st != ACHR_OK) return st;
+    const int P = a_in.P, T = a_in.T, k = a_in.check_period;
+    if (P <= 0) return ACHR_OK;
+    const int cap = std::min(P, kDeferChunk);
+    const int segments = T / k + 3;
+    st = ensure_defer(ctx, cap, segments);
+    if (st != ACHR_OK) return st;
+    DeferState &D = *ctx->defer;
+    const ReprojState &R = *ctx->reproj;
+    const int passes = ctx->opt.reprojection_passes > 0 ? ctx->opt.reprojection_passes : 2;
+
+    int dev = 0, sms = 0, per_sm = 0;
+    DEFER_TRY(cudaGetDevice(&dev));
+    DEFER_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const size_t corr_smem = sizeof(double) * (size_t)D.ld + sizeof(float) * (size_t)D.ldz;
+    DEFER_TRY(cudaFuncSetAttribute(defer_correct_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)corr_smem));
+    DEFER_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, defer_correct_kernel, kCorrThreads, corr_smem));
+    if (per_sm < 1) return set_err(ACHR_ERR_UNSUPPORTED, "model too large for the batched reprojection's update");
+
+    ctx->last_segments = 0;
+    for (int c0 = 0; c0 < P; c0 += cap) {
+        const int pc = std::min(cap, P - c0);
+        DEFER_TRY(cudaMemsetAsync(D.flags.p, 0, sizeof(unsigned) * (size_t)pc, s));
+        DEFER_TRY(cudaMemsetAsync(D.any.p, 0, sizeof(unsigned long long) * (size_t)segments, s));
+        ChainArgs a = a_in;
+        a.P = pc;
+        a.chain_offset = a_in.chain_offset + (unsigned long long)c0;
+        a.out = a_in.out + c0;  // columns c0.. of the n x P row-major output
+        a.pinv32 = nullptr;     // no reprojection inside the chain kernel
+        a.seg = 1;
+        a.seg_x = D.x.p;
+        a.seg_A = D.A.p;
+        a.ld_seg = D.ld;
+        a.seg_flags = D.flags.p;
+        a.row_orig = D.row_orig.p;
+        a.seg_Rh = D.Rh.p;
+        a.seg_Rl = D.Rl.p;
+        a.kpad = D.kpad;
+        const int corr_grid = (int)std::min<long long>((long long)sms * per_sm, pc);
+        int s0 = 0, seg = 0;
+        for (;;) {
+            // The launch runs to the first check step at or after s0 (the reference
+            // checks at steps that are multiples of the period, ACHRCuda.cu:325).
+            const int c = (s0 + k - 1) / k * k;
+            const bool ends_on_check = c <= T - 1;
+            a.step0 = s0;
+            a.T = ends_on_check ? c - s0 + 1 : T - s0;
+            a.seg_final = ends_on_check ? 0 : 1;
+            a.seg_any = D.any.p + seg;
+            DEFER_TRY(launch_chains(a, threads_per_chain, s));
+            ++ctx->last_segments;
+            if (!ends_on_check) break;
+            for (int pass = 0; pass < passes; ++pass) {
+                TcGemm g{pc, R.m, R.kpad, 3, D.Rh.p, D.Rl.p, (long long)R.kpad, R.Bh.p, R.Bl.p, (long long)R.kpad,
+                         D.Z.p, (long long)D.ldz};
+                g.gate = D.any.p + seg;  // skipped when no chain of this launch needs a reprojection
+                g.gate_max = 0;
+                if (const char *why = tc_gemm_check(g)) return set_err(ACHR_ERR_INVALID, why);
+                DEFER_TRY(launch_tc_gemm(g, a_in.counters + CNT_ERROR, s));
+                defer_correct_kernel<<<(unsigned)corr_grid, kCorrThreads, corr_smem, s>>>(
+                    ctx->n, ctx->m, R.kpad, pc, D.x.p, D.ld, D.flags.p, D.Z.p, D.ldz, R.cp.p, R.ri.p, R.cv.p, R.rp.p,
+                    R.ci.p, R.rv.p, reinterpret_cast<__nv_bfloat16 *>(D.Rh.p),
+                    reinterpret_cast<__nv_bfloat16 *>(D.Rl.p), pass + 1 < passes ? 1 : 0);
+                DEFER_TRY(cudaGetLastError());
+            }
+            ++seg;
+            s0 = c + 1;
+            if (s0 >= T) {  // the run's last step was a check step: a launch that only finishes it
+                a.step0 = T;
+                a.T = 0;
+                a.seg_final = 1;
+                a.seg_any = D.any.p + seg;
+                DEFER_TRY(launch_chains(a, threads_per_chain, s));
+                ++ctx->last_segments;
+                break;
+            }
+        }
+    }
+    return ACHR_OK;
+}
+
+}  // namespace achr

@@ -78,6 +78,33 @@ struct ChainArgs {
     unsigned long long *counters;  // CNT_SLOTS entries
     unsigned long long wait_ns;    // limit of the wait for a staged column (0: the default, 2 s)
     int wait_never;                // 1: that wait is on a barrier nothing completes (tests the timeout)
+    // Segmented sampling (achr_defer.cu): the reference's per-chain reprojection
+    // is deferred to a batched pass between launches.  A launch runs the steps
+    // [step0, step0 + T) of every chain; a check step ends the chain's launch
+    // right after x <- x + t u: the kernel writes S x (as BF16 hi/lo, rows in
+    // the model's order) for a chain whose residual exceeds residual_tol, and
+    // the point and centre accumulator to chain-major state; the next launch
+    // (after the batched reprojection has updated the points) clips the point
+    // and adds it to the accumulator before its first step, as the reference
+    // does after reprojecting (ACHRCuda.cu:338-350).
+    int seg;                       // 1: segmented launch
+    int seg_final;                 // 1: this launch holds the run's last step (emit points, diagnostics)
+    double *seg_x, *seg_A;         // P x ld_seg chain-major points and centre accumulators
+    long long ld_seg;
+    unsigned *seg_flags;           // per chain, SEG_* bits
+    unsigned long long *seg_any;   // set to 1 when a chain of this launch needs a reprojection
+    const int *row_orig;           // device row q of S -> row in the model's order
+    unsigned short *seg_Rh, *seg_Rl;  // P x kpad BF16 bits: hi and lo parts of S x
+    int kpad;
+};
+
+// Per-chain state bits of segmented sampling.
+enum SegFlag : unsigned {
+    SEG_STARTED = 1u,   // the chain-major state holds the chain's point and accumulator
+    SEG_ACCEPTED = 2u,  // at least one step accepted
+    SEG_STUCK = 4u,     // stopped after max_attempts rejections
+    SEG_PENDING = 8u,   // the last launch ended after a check step's update: clip and add to the centre next
+    SEG_REPROJ = 16u,   // that check found max|S x| > residual_tol: the batched pass reprojects the point
 };
 
 // FP32 rounding of a double toward +inf / -inf (host side).

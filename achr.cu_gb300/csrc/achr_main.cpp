@@ -11,7 +11,9 @@
 //   --centre cuda|matlab  centre weights (ACHRCuda.cu:347-348 or ACHRSamplerMOD.m:174)
 //   --threads-per-chain N
 //   --check-period N    residual check every N steps (default 10, ACHRCuda.cu:325; 0 = never)
-//   --reproject nnt|residual  per-chain reprojection as N (N^T x) or through the residual
+//   --reproject auto|nnt|residual|deferred  reprojection as N (N^T x) or through the residual in
+//                             the chain kernel, or deferred to a batched tensor-core pass
+//   --reprojection-passes N   passes of the deferred reprojection (default 2)
 //                       (default: chosen by model size)
 //   --bracket-pass merged|separate  ratio-test brackets in the direction pass (default) or in a
 //                       pass of their own; the points are the same
@@ -55,7 +57,8 @@ int main(int argc, char **argv) {
         std::fprintf(stderr,
                      "usage: %s model.mps warmuppoints.csv nFiles nPoints nSteps [--seed S] [--mode reference|feasible]"
                      " [--null sts|svd] [--centre cuda|matlab] [--threads-per-chain N] [--check-period N]"
-                     " [--reproject nnt|residual] [--bracket-pass merged|separate] [--writer-threads N]"
+                     " [--reproject auto|nnt|residual|deferred] [--reprojection-passes N] [--bracket-pass merged|separate]"
+                     " [--writer-threads N]"
                      " [--report file.json]\n",
                      argv[0]);
         return 2;
@@ -103,7 +106,13 @@ int main(int argc, char **argv) {
             std::string m = need();
             if (m == "nnt") opt.reproject_form = 1;
             else if (m == "residual") opt.reproject_form = 2;
+            else if (m == "deferred") opt.reproject_form = 3;
+            else if (m == "auto") opt.reproject_form = 0;
             else return std::fprintf(stderr, "ACHRCuda: bad --reproject\n"), 2;
+        } else if (f == "--reprojection-passes") {
+            if (!parse_int(need(), v) || v < 1 || v > 8)
+                return std::fprintf(stderr, "ACHRCuda: bad --reprojection-passes\n"), 2;
+            opt.reprojection_passes = (int32_t)v;
         } else if (f == "--bracket-pass") {
             std::string m = need();
             if (m == "merged") opt.bracket_pass = 0;

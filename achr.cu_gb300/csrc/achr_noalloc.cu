@@ -219,15 +219,15 @@ extern "C" achr_status achr_sample_noalloc(const achr_device_model *m, const ach
     if (chain_offset + (uint64_t)n_points < chain_offset) return fail(ACHR_ERR_INVALID, "chain ids overflow");
     if (opt.mode != ACHR_MODE_REFERENCE && opt.mode != ACHR_MODE_FEASIBLE) return fail(ACHR_ERR_INVALID, "unknown mode");
     if (opt.check_period < 0 || opt.max_attempts <= 0 || (opt.centre_offset != 0 && opt.centre_offset != 1) ||
-        (opt.bracket_pass != 0 && opt.bracket_pass != 1) || opt.reproject_form < 0 || opt.reproject_form > 2)
+        (opt.bracket_pass != 0 && opt.bracket_pass != 1) || opt.reproject_form < 0 || opt.reproject_form > 3)
         return fail(ACHR_ERR_INVALID, "bad options");
     if (!(opt.residual_tol >= 0) || !(opt.max_min_tol >= 0) || !(opt.u_tol >= 0) || !(opt.d_tol >= 0) ||
         !(opt.feasibility_tol >= 0))
         return fail(ACHR_ERR_INVALID, "tolerances must be non-negative");
-    if (opt.reproject_form == 2)
+    if (opt.reproject_form == 2 || opt.reproject_form == 3)
         return fail(ACHR_ERR_UNSUPPORTED,
-                    "achr_sample_noalloc reprojects as N (N^T x) in FP64; the residual form (reproject_form = 2) "
-                    "needs a pseudo-inverse of S S^T that only a context builds");
+                    "achr_sample_noalloc reprojects as N (N^T x) in FP64; the residual and deferred forms "
+                    "(reproject_form 2 and 3) need a pseudo-inverse of S S^T and buffers that only a context builds");
     const int np = achr::chain_padded_length(n, opt.threads_per_chain);
     if (np == 0 || np > kMaxRxns) return fail(ACHR_ERR_UNSUPPORTED, "no chain-kernel configuration for this size");
     const int prep_blocks = (np + kPrepThreads - 1) / kPrepThreads;

@@ -41,18 +41,6 @@ extern "C" void achr_io_set_error(const char *msg);
 
 namespace achr {
 
-struct ReprojState {
-    int m = 0, n = 0, kpad = 0, rank = 0, device = 0;
-    double lam_max = 0.0, lam_min = 0.0;
-    DevBuf<__nv_bfloat16> Bh, Bl;  // m x kpad row-major: (S S^T)^+ split into hi + lo
-    DevBuf<int> rp, ci, cp, ri;    // CSR and CSC of S (original row order)
-    DevBuf<double> rv, cv;
-    DevBuf<__nv_bfloat16> Rh, Rl;  // chunk x kpad: residuals of a chunk of chains, hi + lo
-    DevBuf<float> Z;               // m x chunk: B r for the chunk
-    int chunk_cap = 0;
-    DevBuf<unsigned long long> flags;  // [1] max|Sx| bits after, [2] device error bits, [8 + r * chunks + c] round r, chunk c
-};
-
 void reproj_free(ReprojState *r) { delete r; }
 
 namespace {
@@ -326,6 +314,8 @@ achr_status build_reproj(achr_ctx *ctx, ReprojState &R, bool want_pinv32 = false
     return ACHR_OK;
 }
 
+}  // namespace
+
 achr_status ensure_reproj(achr_ctx *ctx) {
     if (ctx->reproj) return ACHR_OK;
     ReprojState *R = new (std::nothrow) ReprojState();
@@ -338,6 +328,8 @@ achr_status ensure_reproj(achr_ctx *ctx) {
     ctx->reproj = R;
     return ACHR_OK;
 }
+
+namespace {
 
 achr_status ensure_chunk(ReprojState &R, int chunk) {
     if (chunk <= R.chunk_cap) return ACHR_OK;

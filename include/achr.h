@@ -77,11 +77,24 @@ typedef struct {
     int32_t threads_per_chain;/* 0: chosen by size; else 32, 64, 128, 256, 320, 384 or 512 threads per chain
                                  (320 and 384 hold up to 3840 reactions) */
     int32_t reproject_form;   /* per-chain reprojection x <- N (N^T x) (ACHRCuda.cu:208-230) computed as
-                                 0: chosen by size (the residual form when n_rxns x null_dim >= 4e6),
-                                 1: N (N^T x) in FP64,
-                                 2: x - S^T (S S^T)^+ S x, the pseudo-inverse product in FP32 on the
-                                    residual (equal in exact arithmetic; m^2 FP32 instead of 4 n d FP64
-                                    operations); needs n_mets <= 8192 */
+                                 0: chosen by the inputs: deferred (3) when the warmup points carry a
+                                    residual max|S w| > residual_tol / 8 (a %f-rounded CSV: nearly every
+                                    check then reprojects) and n_rxns x null_dim >= 2.5e5; otherwise in the
+                                    chain kernel, as 2 when n_rxns x null_dim >= 4e6, else as 1,
+                                 1: N (N^T x) in FP64 in the chain kernel,
+                                 2: x - S^T (S S^T)^+ S x in the chain kernel, the pseudo-inverse product
+                                    in FP32 on the residual (equal in exact arithmetic; m^2 FP32 instead
+                                    of 4 n d FP64 operations); needs n_mets <= 8192,
+                                 3: deferred: every chain's launch stops after a check step's update,
+                                    and the chains whose residual exceeds residual_tol are reprojected
+                                    together, x <- x - S^T (S S^T)^+ S x with S x and the update in FP64
+                                    and the dense product on the tensor cores (three BF16 split
+                                    products), repeated reprojection_passes times (each pass multiplies
+                                    the remaining error by about 1e-3); then the clip and the centre
+                                    update of that step, as the reference orders them; needs
+                                    n_mets <= the chain kernel's padded length (achr_sample and
+                                    achr_sample_device only; resumed, batched and hit-and-run launches
+                                    reproject in the chain kernel) */
     double residual_tol;      /* 1e-9 (ACHRCuda.cu:338) */
     double max_min_tol;       /* 1e-9 (ACHRCuda.cu:505) */
     double u_tol;             /* 1e-9 (ACHRCuda.cu:508) */
@@ -97,6 +110,7 @@ typedef struct {
                                  bounded through the box (or the longest hit-and-run direction); a step
                                  whose threshold exceeds the bound, or a model with an infinite bound,
                                  uses a separate pass.  1: always a separate pass.  Results are equal. */
+    int32_t reprojection_passes; /* passes of the deferred reprojection (reproject_form 3), 1..8; 0: 2 */
 } achr_options;
 
 typedef struct {
@@ -110,6 +124,8 @@ typedef struct {
     double max_residual;      /* max ||S v||_inf over emitted points (FEASIBLE mode) */
     double max_bound_violation; /* max over emitted points of max(lb - v, v - ub, 0) */
     double kernel_ms;         /* device time of the sampling launch(es) */
+    int64_t segments;         /* chain-kernel launches of deferred-reprojection sampling (reproject_form 3,
+                                 or 0 choosing it); 0 when reprojections ran inside the chain kernel */
 } achr_stats;
 
 typedef struct achr_ctx achr_ctx;
@@ -375,7 +391,7 @@ typedef struct {
  * ACHR_ERR_INVALID.  What differs from a context: the null space is the
  * caller's (as with achr_set_null_space); the residual check reads the
  * caller's CSR rather than a sliced-ELL copy (same sums); reprojection is
- * N (N^T x) in FP64 (reproject_form 2 gives ACHR_ERR_UNSUPPORTED); in
+ * N (N^T x) in FP64 (reproject_form 2 or 3 gives ACHR_ERR_UNSUPPORTED); in
  * ACHR_MODE_FEASIBLE only the final projection of emitted points is applied
  * (the warmup points are used as given).  Synchronises the stream and reports
  * an expired column wait as ACHR_ERR_TIMEOUT; stats->kernel_ms is 0. */

@@ -72,7 +72,7 @@ def test_create_validates_before_gpu_work(native, pkg):
     warm = np.zeros(3)
     wp = warm.ctypes.data_as(C.POINTER(C.c_double))
     ctx = C.c_void_p()
-    for field, value in (("check_period", -1), ("reproject_form", 3), ("threads_per_chain", 100),
+    for field, value in (("check_period", -1), ("reproject_form", 4), ("reprojection_passes", 9), ("threads_per_chain", 100),
                          ("max_attempts", 0), ("centre_offset", 2), ("mode", 7), ("bracket_pass", 2)):
         o = pkg.default_options()
         setattr(o, field, value)
