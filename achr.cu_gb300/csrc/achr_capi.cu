@@ -175,7 +175,8 @@ achr_status validate_options(const achr_options &o) {
 // n * sigma_0 * 2.2204e-16; the basis is every eigenvector whose eigenvalue
 // magnitude is below the cutoff (ACHRCuda.cu:459-489).  If no value falls
 // below the cutoff the reference keeps istart = 0 and uses all n columns.
-achr_status null_space_sts(int n, int m, const std::vector<double> &denseS, std::vector<double> &N, int &d) {
+achr_status null_space_sts(int n, int m, const std::vector<double> &denseS, std::vector<double> &N, int &d,
+                           double &kappa) {
     DevBuf<double> dS, dStS, dW, work;
     DevBuf<int> info;
     ACHR_CUDA_TRY(dS.upload(denseS.data(), (size_t)m * n));
@@ -214,8 +215,13 @@ achr_status null_space_sts(int n, int m, const std::vector<double> &denseS, std:
     for (int i = 0; i < n; ++i) smax = std::max(smax, std::fabs(lam[i]));
     const double tol = (double)n * smax * 2.2204e-16;
     std::vector<int> cols;
-    for (int i = 0; i < n; ++i)
+    double lkept = 0.0;  // smallest eigenvalue above the cutoff
+    for (int i = 0; i < n; ++i) {
         if (std::fabs(lam[i]) < tol) cols.push_back(i);
+        else if (lkept == 0.0 || std::fabs(lam[i]) < lkept) lkept = std::fabs(lam[i]);
+    }
+    // condition number of S S^T on its range (the same non-zero spectrum as S^T S)
+    kappa = lkept > 0.0 ? smax / lkept : 1.0;
     if (cols.empty())
         for (int i = 0; i < n; ++i) cols.push_back(i);
     d = (int)cols.size();
@@ -228,7 +234,8 @@ achr_status null_space_sts(int n, int m, const std::vector<double> &denseS, std:
 // Null space from the SVD of S^T (n x m, n >= m as cuSOLVER's gesvd needs):
 // left singular vectors beyond the numerical rank span null(S).  Cutoff
 // max(m,n) * sigma_0 * 2.2204e-16 on the singular values of S.
-achr_status null_space_svd_s(int n, int m, const std::vector<double> &denseS, std::vector<double> &N, int &d) {
+achr_status null_space_svd_s(int n, int m, const std::vector<double> &denseS, std::vector<double> &N, int &d,
+                             double &kappa) {
     if (n < m) return fail(ACHR_ERR_UNSUPPORTED, "ACHR_NULL_SVD_S needs n_rxns >= n_mets");
     std::vector<double> St((size_t)n * m);
     for (int i = 0; i < m; ++i)
@@ -267,6 +274,7 @@ achr_status null_space_svd_s(int n, int m, const std::vector<double> &denseS, st
     int rank = 0;
     for (int i = 0; i < m; ++i)
         if (sig[i] >= tol && sig[i] > 0.0) ++rank;
+    kappa = rank > 0 ? (sig[0] / sig[(size_t)rank - 1]) * (sig[0] / sig[(size_t)rank - 1]) : 1.0;
     d = n - rank;
     N.assign((size_t)n * (d > 0 ? d : 0), 0.0);
     for (int j = 0; j < d; ++j)
@@ -344,6 +352,8 @@ achr_status read_counters(achr_ctx *ctx, achr_stats *stats, float ms) {
         return fail(ACHR_ERR_TIMEOUT, "a warmup-column copy did not complete within its wait limit");
     if (c[achr::CNT_ERROR] & achr::ERR_TC_TIMEOUT)
         return fail(ACHR_ERR_TIMEOUT, "a tensor-core pipeline wait of the batched reprojection expired");
+    if (c[achr::CNT_ERROR] & achr::ERR_DEFER_DIVERGED)
+        return fail(ACHR_ERR_NUMERIC, "a deferred reprojection left max|S x| above residual_tol after its last pass");
     if (stats) {
         stats->accepted = (int64_t)c[achr::CNT_ACCEPTED];
         stats->rejected = (int64_t)c[achr::CNT_REJECTED];
@@ -547,8 +557,8 @@ achr_status achr_create(const achr_model *model, const double *warmup, int32_t n
         Nh.assign((size_t)n * n, 0.0);
         for (int i = 0; i < n; ++i) Nh[(size_t)i * n + i] = 1.0;
     } else {
-        st = (opt.null_space == ACHR_NULL_SVD_S) ? null_space_svd_s(n, m, denseS, Nh, d)
-                                                 : null_space_sts(n, m, denseS, Nh, d);
+        st = (opt.null_space == ACHR_NULL_SVD_S) ? null_space_svd_s(n, m, denseS, Nh, d, ctx->kappa_sst)
+                                                 : null_space_sts(n, m, denseS, Nh, d, ctx->kappa_sst);
         if (st != ACHR_OK) return st;
     }
     st = upload_null_space(ctx, Nh.data(), d);
@@ -623,7 +633,9 @@ achr_status achr_sample_device(achr_ctx *ctx, uint64_t seed, uint64_t chain_offs
         ctx->m > 0) {
         if (e0) cudaEventDestroy(e0);
         if (e1) cudaEventDestroy(e1);
-        return fail(ACHR_ERR_UNSUPPORTED, "deferred reprojection needs n_mets <= the chain kernel's padded length");
+        return fail(ACHR_ERR_UNSUPPORTED,
+                    "deferred reprojection needs n_mets <= the chain kernel's padded length and a condition number "
+                    "of S S^T of at most 2e4 (its BF16-split passes converge only then)");
     }
     cudaError_t e = cudaSuccess;
     achr_status dst = ACHR_OK;
@@ -792,11 +804,15 @@ achr_status achr_sample_resume(achr_ctx *ctx, uint64_t seed, uint64_t chain_offs
         ACHR_CUDA_TRY(cudaEventCreate(&e1));
         ACHR_CUDA_TRY(cudaEventRecord(e0, s));
     }
-    cudaError_t e = achr::launch_chains(a, ctx->opt.threads_per_chain, s);
-    if (e != cudaSuccess) {
+    const bool deferred = achr::defer_selected(ctx) && n_points > 0 && n_steps > 0;
+    cudaError_t e = cudaSuccess;
+    achr_status dst = ACHR_OK;
+    if (deferred) dst = achr::defer_sample(ctx, a, ctx->opt.threads_per_chain, s);
+    else e = achr::launch_chains(a, ctx->opt.threads_per_chain, s);
+    if (e != cudaSuccess || dst != ACHR_OK) {
         if (e0) cudaEventDestroy(e0);
         if (e1) cudaEventDestroy(e1);
-        return cuda_fail(e, "chain kernel launch");
+        return dst != ACHR_OK ? dst : cuda_fail(e, "chain kernel launch");
     }
     if (!stats) return ACHR_OK;
     ACHR_CUDA_TRY(cudaEventRecord(e1, s));
@@ -805,7 +821,9 @@ achr_status achr_sample_resume(achr_ctx *ctx, uint64_t seed, uint64_t chain_offs
     cudaEventElapsedTime(&ms, e0, e1);
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    return read_counters(ctx, stats, ms);
+    achr_status rst = read_counters(ctx, stats, ms);
+    if (rst == ACHR_OK) stats->segments = deferred ? ctx->last_segments : 0;
+    return rst;
 }
 
 achr_status achr_sample(achr_ctx *ctx, uint64_t seed, uint64_t chain_offset, int32_t n_points, int32_t n_steps,

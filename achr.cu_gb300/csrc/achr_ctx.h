@@ -103,6 +103,7 @@ struct achr_ctx {
     achr::ReprojState *reproj = nullptr;  // batched reprojection operator, built on first use
     achr::DeferState *defer = nullptr;    // buffers of segmented sampling, built on first use
     double warmup_residual = 0.0;         // max |S w|_inf over the warmup points (as sampled)
+    double kappa_sst = 1.0;               // condition number of S S^T on its range (from the null-space set-up)
     long long last_segments = 0;          // chain-kernel launches of the last deferred-reprojection run
     achr::DevBuf<double> dirs;   // hit-and-run direction pool, n x n_dirs (leading dimension ldw)
     int n_dirs = 0;              // 0: ACHR directions (warmup point minus centre)

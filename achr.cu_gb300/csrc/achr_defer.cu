@@ -23,8 +23,11 @@
 // products, FP32 accumulation, achr_tc_gemm.cu) and the update S^T z in FP64.
 // The low-precision product only ever sees the residual, and the update lies
 // in the row space of S, so the null-space part of x is untouched and each
-// further pass multiplies what is left of the row-space part by about 1e-3:
-// two passes leave the point within ~1e-12 of the FP64 projection.  The next
+// further pass multiplies what is left of the row-space part by roughly
+// 1.5e-6 times the condition number of S S^T (about 2e-3 at 1265); a chain
+// takes passes until max|S x| <= residual_tol / 100, which puts it within
+// that over the smallest singular value of S of the FP64 projection (models
+// with a condition number above 2e4 reproject in the chain kernel).  The next
 // launch of the chain kernel clips each point and adds it to its centre
 // accumulator before the chain's next step, the order the reference uses.
 // The decisions (which chains reproject) are the chain kernel's own FP64
@@ -61,8 +64,10 @@ void defer_free(DeferState *d) { delete d; }
 
 namespace {
 
-constexpr int kDeferChunk = 131072;  // chains per sweep through the segments (bounds the buffers)
+constexpr int kDeferChunk = 131072;        // chains per sweep through the segments (bounds the buffers)
+constexpr double kDeferMaxKappa = 2.0e4;   // largest condition number of S S^T the passes are used for
 constexpr int kCorrThreads = 256;
+constexpr int kMaxPasses = 8;              // passes of one deferred reprojection at most
 
 achr_status set_err(achr_status st, const std::string &msg) {
     achr_io_set_error(msg.c_str());
@@ -75,21 +80,28 @@ achr_status set_err(achr_status st, const std::string &msg) {
         if (e_ != cudaSuccess) return set_err(ACHR_ERR_CUDA, std::string(#expr) + ": " + cudaGetErrorString(e_)); \
     } while (0)
 
-// x <- x - S^T z for every chain flagged SEG_REPROJ (one CTA per chain at a
-// time, chain-major rows so every load and store is coalesced; z from the
-// GEMM's row of that chain), then, for the next pass, S x again (FP64) as
-// BF16 hi/lo into R.  S is read in the model's row order (CSC for S^T z, CSR
-// for S x), matching the rows of B.
+// x <- x - S^T z for every chain still flagged SEG_REPROJ (one CTA per chain
+// at a time, chain-major rows so every load and store is coalesced; z from the
+// GEMM's row of that chain), then S x again in FP64.  A chain whose max|S x|
+// is now within fine_tol is done (its flag is cleared); any other is split into
+// R for the next pass and marks that pass as needed (*next_any).  After the
+// last pass a chain still above residual_tol raises ERR_DEFER_DIVERGED.  S is
+// read in the model's row order (CSC for S^T z, CSR for S x), matching B.
 __global__ void __launch_bounds__(kCorrThreads)
     defer_correct_kernel(int n, int m, int kpad, int P, double *__restrict__ X, long long ldx,
-                         const unsigned *__restrict__ flags, const float *__restrict__ Z, long long ldz,
+                         unsigned *__restrict__ flags, const float *__restrict__ Z, long long ldz,
                          const int *__restrict__ cp, const int *__restrict__ ri, const double *__restrict__ cv,
                          const int *__restrict__ rp, const int *__restrict__ ci, const double *__restrict__ rv,
-                         __nv_bfloat16 *__restrict__ Rh, __nv_bfloat16 *__restrict__ Rl, int want_residual) {
+                         __nv_bfloat16 *__restrict__ Rh, __nv_bfloat16 *__restrict__ Rl, double fine_tol,
+                         double residual_tol, int last, unsigned long long *next_any,
+                         unsigned long long *counters) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ unsigned long long wmax[kCorrThreads / 32];
     double *xsm = reinterpret_cast<double *>(smem_raw);
     float *zs = reinterpret_cast<float *>(xsm + ldx);
-    const int tid = threadIdx.x;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const unsigned long long fine_bits = (unsigned long long)__double_as_longlong(fine_tol);
+    const unsigned long long tol_bits = (unsigned long long)__double_as_longlong(residual_tol);
     for (int p = blockIdx.x; p < P; p += gridDim.x) {
         if (!(flags[p] & SEG_REPROJ)) continue;  // uniform over the block
         const float *zp = Z + (size_t)p * (size_t)ldz;
@@ -105,15 +117,31 @@ __global__ void __launch_bounds__(kCorrThreads)
             xsm[j] = xv;
         }
         __syncthreads();
-        if (want_residual) {
-            __nv_bfloat16 *rh = Rh + (size_t)p * (size_t)kpad, *rl = Rl + (size_t)p * (size_t)kpad;
-            for (int i = tid; i < m; i += kCorrThreads) {
-                double acc = 0.0;
-                const int q1 = __ldg(rp + i + 1);
-                for (int q = __ldg(rp + i); q < q1; ++q) acc = fma(__ldg(rv + q), xsm[__ldg(ci + q)], acc);
+        __nv_bfloat16 *rh = Rh + (size_t)p * (size_t)kpad, *rl = Rl + (size_t)p * (size_t)kpad;
+        unsigned long long mx = 0;
+        for (int i = tid; i < m; i += kCorrThreads) {
+            double acc = 0.0;
+            const int q1 = __ldg(rp + i + 1);
+            for (int q = __ldg(rp + i); q < q1; ++q) acc = fma(__ldg(rv + q), xsm[__ldg(ci + q)], acc);
+            mx = max(mx, (unsigned long long)__double_as_longlong(acc) & 0x7FFFFFFFFFFFFFFFull);
+            if (!last) {
                 const __nv_bfloat16 hi = __double2bfloat16(acc);
                 rh[i] = hi;
                 rl[i] = __double2bfloat16(acc - (double)__bfloat162float(hi));
+            }
+        }
+#pragma unroll
+        for (int o = 16; o; o >>= 1) mx = max(mx, (unsigned long long)__shfl_xor_sync(0xffffffffu, mx, o));
+        if (lane == 0) wmax[warp] = mx;
+        __syncthreads();
+        if (tid == 0) {
+            for (int w = 1; w < kCorrThreads / 32; ++w) mx = max(mx, wmax[w]);
+            if (mx <= fine_bits) {
+                flags[p] &= ~SEG_REPROJ;  // converged
+            } else if (!last) {
+                if (*next_any == 0ull) atomicOr(next_any, 1ull);
+            } else if (mx > tol_bits) {
+                atomicOr(counters + CNT_ERROR, (unsigned long long)ERR_DEFER_DIVERGED);
             }
         }
         __syncthreads();
@@ -161,6 +189,10 @@ bool defer_selected(const achr_ctx *ctx) {
     if (o.check_period <= 0 || ctx->m <= 0) return false;
     const int np = chain_padded_length(ctx->n, o.threads_per_chain);
     if (np == 0 || ctx->m > np) return false;  // S x is staged in the chain kernel's column buffer
+    // Each BF16-split pass multiplies the remaining error by roughly 1.5e-6 times the
+    // condition number of S S^T (measured: 1.9e-3 at 1265); beyond 2e4 the passes
+    // converge too slowly to be worth it, and far beyond they diverge.
+    if (ctx->kappa_sst > kDeferMaxKappa) return false;
     if (o.reproject_form == 3) return true;
     if (o.reproject_form != 0 || ctx->n_dirs > 0) return false;
     return ctx->warmup_residual > o.residual_tol / 8.0 && (double)ctx->n * (double)ctx->d >= 2.5e5;
@@ -169,15 +201,20 @@ bool defer_selected(const achr_ctx *ctx) {
 achr_status defer_sample(achr_ctx *ctx, const ChainArgs &a_in, int threads_per_chain, cudaStream_t s) {
     achr_status st = ensure_reproj(ctx);
     if (st != ACHR_OK) return st;
-    const int P = a_in.P, T = a_in.T, k = a_in.check_period;
+    // Steps [S0, E) of every chain (S0 > 0: chains resumed from a_in.x_in / A_in).
+    const int P = a_in.P, S0 = a_in.step0, E = a_in.step0 + a_in.T, k = a_in.check_period;
     if (P <= 0) return ACHR_OK;
     const int cap = std::min(P, kDeferChunk);
-    const int segments = T / k + 3;
-    st = ensure_defer(ctx, cap, segments);
+    const int segments = E / k - S0 / k + 3;
+    // one gate word per launch and pass: [seg * (kMaxPasses + 1) + pass]
+    st = ensure_defer(ctx, cap, segments * (kMaxPasses + 1));
     if (st != ACHR_OK) return st;
     DeferState &D = *ctx->defer;
     const ReprojState &R = *ctx->reproj;
-    const int passes = ctx->opt.reprojection_passes > 0 ? ctx->opt.reprojection_passes : 2;
+    const int passes = ctx->opt.reprojection_passes > 0 ? ctx->opt.reprojection_passes : kMaxPasses;
+    // A chain's pass sequence ends once max|S x| <= residual_tol / 100: the point is then within
+    // about that over the smallest singular value of S of the FP64 projection.
+    const double fine_tol = ctx->opt.residual_tol * 0.01;
 
     int dev = 0, sms = 0, per_sm = 0;
     DEFER_TRY(cudaGetDevice(&dev));
@@ -192,11 +229,14 @@ achr_status defer_sample(achr_ctx *ctx, const ChainArgs &a_in, int threads_per_c
     for (int c0 = 0; c0 < P; c0 += cap) {
         const int pc = std::min(cap, P - c0);
         DEFER_TRY(cudaMemsetAsync(D.flags.p, 0, sizeof(unsigned) * (size_t)pc, s));
-        DEFER_TRY(cudaMemsetAsync(D.any.p, 0, sizeof(unsigned long long) * (size_t)segments, s));
+        DEFER_TRY(cudaMemsetAsync(D.any.p, 0, sizeof(unsigned long long) * (size_t)segments * (kMaxPasses + 1), s));
         ChainArgs a = a_in;
         a.P = pc;
         a.chain_offset = a_in.chain_offset + (unsigned long long)c0;
-        a.out = a_in.out + c0;  // columns c0.. of the n x P row-major output
+        a.out = a_in.out + c0;  // columns c0.. of the n x P row-major output (and state, when resumed)
+        if (a_in.x_in) a.x_in = a_in.x_in + c0;
+        if (a_in.A_in) a.A_in = a_in.A_in + c0;
+        if (a_in.A_out) a.A_out = a_in.A_out + c0;
         a.pinv32 = nullptr;     // no reprojection inside the chain kernel
         a.seg = 1;
         a.seg_x = D.x.p;
@@ -208,39 +248,41 @@ achr_status defer_sample(achr_ctx *ctx, const ChainArgs &a_in, int threads_per_c
         a.seg_Rl = D.Rl.p;
         a.kpad = D.kpad;
         const int corr_grid = (int)std::min<long long>((long long)sms * per_sm, pc);
-        int s0 = 0, seg = 0;
+        int s0 = S0, seg = 0;
         for (;;) {
             // The launch runs to the first check step at or after s0 (the reference
             // checks at steps that are multiples of the period, ACHRCuda.cu:325).
-            const int c = (s0 + k - 1) / k * k;
-            const bool ends_on_check = c <= T - 1;
+            const int c = (int)(((long long)s0 + k - 1) / k * k);
+            const bool ends_on_check = c <= E - 1;
             a.step0 = s0;
-            a.T = ends_on_check ? c - s0 + 1 : T - s0;
+            a.T = ends_on_check ? c - s0 + 1 : E - s0;
             a.seg_final = ends_on_check ? 0 : 1;
-            a.seg_any = D.any.p + seg;
+            unsigned long long *gate = D.any.p + (size_t)seg * (kMaxPasses + 1);
+            a.seg_any = gate;  // pass 0 is needed when some chain's check fired
             DEFER_TRY(launch_chains(a, threads_per_chain, s));
             ++ctx->last_segments;
             if (!ends_on_check) break;
             for (int pass = 0; pass < passes; ++pass) {
                 TcGemm g{pc, R.m, R.kpad, 3, D.Rh.p, D.Rl.p, (long long)R.kpad, R.Bh.p, R.Bl.p, (long long)R.kpad,
                          D.Z.p, (long long)D.ldz};
-                g.gate = D.any.p + seg;  // skipped when no chain of this launch needs a reprojection
+                g.gate = gate + pass;  // skipped when no chain needs this pass
                 g.gate_max = 0;
                 if (const char *why = tc_gemm_check(g)) return set_err(ACHR_ERR_INVALID, why);
                 DEFER_TRY(launch_tc_gemm(g, a_in.counters + CNT_ERROR, s));
                 defer_correct_kernel<<<(unsigned)corr_grid, kCorrThreads, corr_smem, s>>>(
                     ctx->n, ctx->m, R.kpad, pc, D.x.p, D.ld, D.flags.p, D.Z.p, D.ldz, R.cp.p, R.ri.p, R.cv.p, R.rp.p,
                     R.ci.p, R.rv.p, reinterpret_cast<__nv_bfloat16 *>(D.Rh.p),
-                    reinterpret_cast<__nv_bfloat16 *>(D.Rl.p), pass + 1 < passes ? 1 : 0);
+                    reinterpret_cast<__nv_bfloat16 *>(D.Rl.p), fine_tol, ctx->opt.residual_tol,
+                    pass + 1 == passes ? 1 : 0, gate + pass + 1, a_in.counters);
                 DEFER_TRY(cudaGetLastError());
             }
             ++seg;
             s0 = c + 1;
-            if (s0 >= T) {  // the run's last step was a check step: a launch that only finishes it
-                a.step0 = T;
+            if (s0 >= E) {  // the run's last step was a check step: a launch that only finishes it
+                a.step0 = E;
                 a.T = 0;
                 a.seg_final = 1;
-                a.seg_any = D.any.p + seg;
+                a.seg_any = D.any.p + (size_t)seg * (kMaxPasses + 1);
                 DEFER_TRY(launch_chains(a, threads_per_chain, s));
                 ++ctx->last_segments;
                 break;

@@ -25,6 +25,7 @@ enum CounterSlot {
 enum DeviceError : unsigned long long {
     ERR_TMA_TIMEOUT = 1ull,
     ERR_TC_TIMEOUT = 2ull,  // a tensor-core GEMM pipeline wait expired
+    ERR_DEFER_DIVERGED = 4ull,  // a deferred reprojection ended with max|S x| > residual_tol
 };
 
 // Everything one chain-sampling launch reads (device pointers) and its scalars.

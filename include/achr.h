@@ -79,8 +79,9 @@ typedef struct {
     int32_t reproject_form;   /* per-chain reprojection x <- N (N^T x) (ACHRCuda.cu:208-230) computed as
                                  0: chosen by the inputs: deferred (3) when the warmup points carry a
                                     residual max|S w| > residual_tol / 8 (a %f-rounded CSV: nearly every
-                                    check then reprojects) and n_rxns x null_dim >= 2.5e5; otherwise in the
-                                    chain kernel, as 2 when n_rxns x null_dim >= 4e6, else as 1,
+                                    check then reprojects), n_rxns x null_dim >= 2.5e5 and form 3's
+                                    conditions hold; otherwise in the chain kernel, as 2 when
+                                    n_rxns x null_dim >= 4e6, else as 1,
                                  1: N (N^T x) in FP64 in the chain kernel,
                                  2: x - S^T (S S^T)^+ S x in the chain kernel, the pseudo-inverse product
                                     in FP32 on the residual (equal in exact arithmetic; m^2 FP32 instead
@@ -89,12 +90,14 @@ typedef struct {
                                     and the chains whose residual exceeds residual_tol are reprojected
                                     together, x <- x - S^T (S S^T)^+ S x with S x and the update in FP64
                                     and the dense product on the tensor cores (three BF16 split
-                                    products), repeated reprojection_passes times (each pass multiplies
-                                    the remaining error by about 1e-3); then the clip and the centre
-                                    update of that step, as the reference orders them; needs
-                                    n_mets <= the chain kernel's padded length (achr_sample and
-                                    achr_sample_device only; resumed, batched and hit-and-run launches
-                                    reproject in the chain kernel) */
+                                    products), repeated per chain until max|S x| <= residual_tol / 100
+                                    (each pass multiplies the remaining error by about 1.5e-6 times the
+                                    condition number of S S^T); then the clip and the centre update of
+                                    that step, as the reference orders them; needs n_mets <= the chain
+                                    kernel's padded length and that condition number <= 2e4 (achr_sample,
+                                    achr_sample_device and achr_sample_resume; batched launches
+                                    reproject in the chain kernel, and so does choice 0 with a
+                                    hit-and-run pool) */
     double residual_tol;      /* 1e-9 (ACHRCuda.cu:338) */
     double max_min_tol;       /* 1e-9 (ACHRCuda.cu:505) */
     double u_tol;             /* 1e-9 (ACHRCuda.cu:508) */
@@ -110,7 +113,8 @@ typedef struct {
                                  bounded through the box (or the longest hit-and-run direction); a step
                                  whose threshold exceeds the bound, or a model with an infinite bound,
                                  uses a separate pass.  1: always a separate pass.  Results are equal. */
-    int32_t reprojection_passes; /* passes of the deferred reprojection (reproject_form 3), 1..8; 0: 2 */
+    int32_t reprojection_passes; /* most passes of one deferred reprojection, 1..8 (0: 8); a chain still
+                                    above residual_tol after the last pass is an ACHR_ERR_NUMERIC */
 } achr_options;
 
 typedef struct {

@@ -99,3 +99,21 @@ def test_deferred_feasible_mode(pkg, small_model, golden):
     assert np.abs(S @ pts).max() <= 1e-8
     lb, ub = golden["lb"][:, None], golden["ub"][:, None]
     assert (pts >= lb - 1e-9).all() and (pts <= ub + 1e-9).all()
+
+
+def test_deferred_resume_in_segments_equals_one_run(deferred):
+    """achr_sample_resume with deferred reprojection: 12 + 9 + 17 steps (the second segment ends on
+    a check step) give the points of one 38-step run, bit for bit."""
+    torch = pytest.importorskip("torch")
+    P, n = 48, deferred.n
+    pts = torch.zeros((n, P), dtype=torch.float64, device="cuda")
+    acc = torch.zeros((n, P), dtype=torch.float64, device="cuda")
+    stream = torch.cuda.current_stream().cuda_stream
+    step = 0
+    for seg, resume in ((12, False), (9, True), (17, True)):
+        st = deferred.sample_resume(P, step, seg, resume, pts.data_ptr(), acc.data_ptr(), P, stream=stream, seed=21,
+                                    chain_offset=5, with_stats=True)
+        assert st["accepted"] == P * seg and st["segments"] > 0
+        step += seg
+    ref, _ = deferred.sample(P, 38, seed=21, chain_offset=5)
+    assert np.array_equal(pts.cpu().numpy(), ref)
