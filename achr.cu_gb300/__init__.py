@@ -120,7 +120,7 @@ class PrecondOptions(C.Structure):
     _fields_ = [
         ("iterations", C.c_int32), ("batch", C.c_int32), ("learning_rate", C.c_float), ("beta1", C.c_float),
         ("beta2", C.c_float), ("eps", C.c_float), ("seed", C.c_uint64), ("init", C.c_int32),
-        ("standardize", C.c_int32),
+        ("standardize", C.c_int32), ("full_batch", C.c_int32),
     ]
 
 

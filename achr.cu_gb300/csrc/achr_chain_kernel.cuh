@@ -352,15 +352,13 @@ __device__ __forceinline__ unsigned long long residual_rows(const ChainArgs &a, 
     return mx;
 }
 
-// BF16 bits of v rounded to nearest (hi) and of the remainder v - hi (lo).
-__device__ __forceinline__ void split_bf16_bits(double v, unsigned short &hi, unsigned short &lo) {
-    const float f = __double2float_rn(v);
-    unsigned u = __float_as_uint(f);
-    // round-to-nearest-even of the FP32 value to its upper 16 bits (finite values)
+// BF16 bits of f rounded to nearest even (hi) and of the remainder f - hi (lo),
+// for finite f; FP32 and integer operations only.
+__device__ __forceinline__ void split_bf16_bits(float f, unsigned short &hi, unsigned short &lo) {
+    const unsigned u = __float_as_uint(f);
     const unsigned hu = (u + 0x7FFFu + ((u >> 16) & 1u)) & 0xFFFF0000u;
     hi = (unsigned short)(hu >> 16);
-    const float rem = __double2float_rn(v - (double)__uint_as_float(hu));
-    unsigned r = __float_as_uint(rem);
+    const unsigned r = __float_as_uint(f - __uint_as_float(hu));
     const unsigned ru = (r + 0x7FFFu + ((r >> 16) & 1u)) & 0xFFFF0000u;
     lo = (unsigned short)(ru >> 16);
 }
@@ -525,6 +523,15 @@ __global__ void __launch_bounds__(BD, (BD <= 384 ? 2 : 1)) achr_chain_kernel(con
         bool seg_pending = false;  // this launch ended the chain after a check step's update
         const bool was_stuck = (sflags & SEG_STUCK) != 0;
         if (was_stuck) stuck = true;  // stopped in an earlier launch: no more steps
+        if (sflags & SEG_CORR) {
+            // The batched passes' correction of this chain (x <- x - S^T z summed over
+            // the passes, in FP32: it is at most the size of the residual's preimage).
+#pragma unroll
+            for (int k = 0; k < EPT; ++k) {
+                const int i = tid + k * BD;
+                if (i < a.n) xs[i] -= (double)a.seg_dx[(size_t)p * (size_t)a.ld_seg + (size_t)i];
+            }
+        }
         if (sflags & SEG_PENDING) {
             // Finish the check step the previous launch ended on (the batched
             // pass has reprojected the point if its residual was above the
@@ -992,12 +999,16 @@ __global__ void __launch_bounds__(BD, (BD <= 384 ? 2 : 1)) achr_chain_kernel(con
                         }
                         unsigned short *rh = a.seg_Rh + (size_t)p * (size_t)a.kpad;
                         unsigned short *rl = a.seg_Rl + (size_t)p * (size_t)a.kpad;
+                        float *r32 = a.seg_r + (size_t)p * (size_t)a.ld_r;
                         for (int q = tid; q < a.m; q += BD) {
+                            // (one FP64 conversion per row; the split itself is FP32)
+                            const float f = __double2float_rn(rr[q]);
                             unsigned short h, l;
-                            split_bf16_bits(rr[q], h, l);
+                            split_bf16_bits(f, h, l);
                             const int row = __ldg(a.row_orig + q);
                             rh[row] = h;
                             rl[row] = l;
+                            r32[row] = f;
                         }
                     }
 #pragma unroll
@@ -1009,7 +1020,8 @@ __global__ void __launch_bounds__(BD, (BD <= 384 ? 2 : 1)) achr_chain_kernel(con
                         }
                     }
                     if (tid == 0) {
-                        a.seg_flags[p] = SEG_STARTED | SEG_ACCEPTED | SEG_PENDING | (reproject ? SEG_REPROJ : 0u);
+                        a.seg_flags[p] =
+                            SEG_STARTED | SEG_ACCEPTED | SEG_PENDING | (reproject ? SEG_REPROJ | SEG_CORR : 0u);
                         ++cnt[CNT_ACCEPTED];
                     }
                     __syncthreads();  // the residual rows in ws are read before the next chain's column lands

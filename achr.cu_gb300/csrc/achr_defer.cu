@@ -12,26 +12,29 @@
 //
 // Here every chain runs to its next check step in one launch of the chain
 // kernel (segmented mode, achr_chain_kernel.cuh), which ends each chain right
-// after the check step's x <- x + t u and leaves, for every chain whose
-// residual exceeds the tolerance, S x (FP64, split into BF16 hi + lo) in a
-// chain-major block R.  The batched pass then applies the same orthogonal
+// after the check step's x <- x + t u and leaves, for every chain whose FP64
+// residual exceeds the tolerance, r = S x in FP32 and split into BF16 hi + lo
+// (chain-major block R).  The batched passes then apply the same orthogonal
 // projector to all of those chains at once,
 //
-//     x <- x - S^T z,   z = B (S x),   B = (S S^T)^+,
+//     x <- x - S^T z,   z = B r,   B = (S S^T)^+,
 //
 // z for every chain as one tensor-core GEMM Z = R B^T (three BF16 split
-// products, FP32 accumulation, achr_tc_gemm.cu) and the update S^T z in FP64.
-// The low-precision product only ever sees the residual, and the update lies
-// in the row space of S, so the null-space part of x is untouched and each
-// further pass multiplies what is left of the row-space part by roughly
-// 1.5e-6 times the condition number of S S^T (about 2e-3 at 1265); a chain
-// takes passes until max|S x| <= residual_tol / 100, which puts it within
-// that over the smallest singular value of S of the FP64 projection (models
-// with a condition number above 2e4 reproject in the chain kernel).  The next
-// launch of the chain kernel clips each point and adds it to its centre
-// accumulator before the chain's next step, the order the reference uses.
-// The decisions (which chains reproject) are the chain kernel's own FP64
-// residual, identical to the check it makes when it reprojects in place.
+// products, FP32 accumulation, achr_tc_gemm.cu); each pass then forms
+// d = S^T z, adds it to the chain's correction dx and tracks r <- r - S d, all
+// in FP32 (they are of the size of the residual, not of x).  The update lies in
+// the row space of S up to FP32 rounding, so the null-space part of x moves by
+// at most ~1e-7 of the correction, and each further pass multiplies what is
+// left of the row-space part by roughly 1.5e-6 times the condition number of
+// S S^T (about 4e-3 at 2572).  A chain takes passes until max|r| falls to
+// max(residual_tol / 100, 1e-5 of the residual its check found), so the
+// corrected point is within about 1e-5 of the correction's own size of the
+// FP64 projection; models whose S S^T has a condition number above 2e4
+// reproject in the chain kernel instead.  The next launch of the chain kernel
+// subtracts dx from the point (FP64), clips it and adds it to its centre
+// accumulator before the chain's next step, the order the reference uses.  The
+// decisions (which chains reproject) are the chain kernel's own FP64 residual,
+// identical to the check it makes when it reprojects in place.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -49,14 +52,18 @@ namespace achr {
 struct DeferState {
     int cap = 0;             // chains the buffers hold
     long long ld = 0;        // leading dimension of the chain-major state (n rounded up to even)
-    int ldz = 0;             // leading dimension of Z (m rounded up to a multiple of 4)
+    int ldz = 0;             // leading dimension of Z and r (m rounded up to a multiple of 4)
     int kpad = 0;            // K of the GEMM: m rounded up to a multiple of 64
     DevBuf<double> x, A;     // cap x ld: points and centre accumulators between launches
     DevBuf<unsigned> flags;  // cap: SEG_* bits
     DevBuf<unsigned short> Rh, Rl;  // cap x kpad BF16 bits: S x of the chains that reproject
     DevBuf<float> Z;         // cap x ldz: B (S x)
+    DevBuf<float> r;         // cap x ldz: S x in FP32, tracked through the passes
+    DevBuf<float> dx;        // cap x ld: the passes' summed correction S^T z
+    DevBuf<float> r0;        // cap: max|S x| of the chain when its check fired
+    DevBuf<float> cv32, rv32;  // CSC and CSR values of S in FP32 (model row order)
     DevBuf<int> row_orig;    // m: device row order of S -> the model's row order
-    DevBuf<unsigned long long> any;  // one word per launch: some chain needs the batched pass
+    DevBuf<unsigned long long> any;  // one word per launch and pass: some chain needs that pass
     int any_cap = 0;
 };
 
@@ -80,67 +87,90 @@ achr_status set_err(achr_status st, const std::string &msg) {
         if (e_ != cudaSuccess) return set_err(ACHR_ERR_CUDA, std::string(#expr) + ": " + cudaGetErrorString(e_)); \
     } while (0)
 
-// x <- x - S^T z for every chain still flagged SEG_REPROJ (one CTA per chain
-// at a time, chain-major rows so every load and store is coalesced; z from the
-// GEMM's row of that chain), then S x again in FP64.  A chain whose max|S x|
-// is now within fine_tol is done (its flag is cleared); any other is split into
-// R for the next pass and marks that pass as needed (*next_any).  After the
-// last pass a chain still above residual_tol raises ERR_DEFER_DIVERGED.  S is
-// read in the model's row order (CSC for S^T z, CSR for S x), matching B.
+__global__ void to_f32_kernel(long long count, const double *__restrict__ in, float *__restrict__ out) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < count) out[t] = __double2float_rn(in[t]);
+}
+
+// One pass for every chain still flagged SEG_REPROJ (a CTA per chain at a
+// time; chain-major rows, so every load and store is coalesced):
+//     d = S^T z,  dx += d,  r <- r - S d,
+// z the chain's row of the GEMM's B (S x).  Everything here is FP32: z itself
+// carries the GEMM's error, d is at most the size of the residual's preimage,
+// and r is tracked from the chain kernel's FP64 residual by subtracting S d,
+// so FP32 rounding stays relative to the residual, not to x; the point itself
+// is touched once, in FP64, when the next launch subtracts dx.  A chain whose
+// max|r| falls to max(fine_tol, 1e-5 max|r0|) is done (flag cleared); any other
+// has r split into R for the next pass and marks that pass as needed.  After
+// the last pass a chain still above residual_tol raises ERR_DEFER_DIVERGED.  S
+// is read in the model's row order (CSC for S^T z, CSR for S d), matching B.
 __global__ void __launch_bounds__(kCorrThreads)
-    defer_correct_kernel(int n, int m, int kpad, int P, double *__restrict__ X, long long ldx,
-                         unsigned *__restrict__ flags, const float *__restrict__ Z, long long ldz,
-                         const int *__restrict__ cp, const int *__restrict__ ri, const double *__restrict__ cv,
-                         const int *__restrict__ rp, const int *__restrict__ ci, const double *__restrict__ rv,
-                         __nv_bfloat16 *__restrict__ Rh, __nv_bfloat16 *__restrict__ Rl, double fine_tol,
-                         double residual_tol, int last, unsigned long long *next_any,
-                         unsigned long long *counters) {
+    defer_pass_kernel(int n, int m, int kpad, int P, int pass, unsigned *__restrict__ flags,
+                      const float *__restrict__ Z, float *__restrict__ Rf, long long ldz, float *__restrict__ DX,
+                      long long ldx, float *__restrict__ r0, const int *__restrict__ cp, const int *__restrict__ ri,
+                      const float *__restrict__ cv, const int *__restrict__ rp, const int *__restrict__ ci,
+                      const float *__restrict__ rv, __nv_bfloat16 *__restrict__ Rh, __nv_bfloat16 *__restrict__ Rl,
+                      float fine_tol, float residual_tol, int last, unsigned long long *next_any,
+                      unsigned long long *counters) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    __shared__ unsigned long long wmax[kCorrThreads / 32];
-    double *xsm = reinterpret_cast<double *>(smem_raw);
-    float *zs = reinterpret_cast<float *>(xsm + ldx);
+    __shared__ float wmax[kCorrThreads / 32][2];
+    float *zs = reinterpret_cast<float *>(smem_raw);
+    float *ds = zs + ldz;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const unsigned long long fine_bits = (unsigned long long)__double_as_longlong(fine_tol);
-    const unsigned long long tol_bits = (unsigned long long)__double_as_longlong(residual_tol);
     for (int p = blockIdx.x; p < P; p += gridDim.x) {
         if (!(flags[p] & SEG_REPROJ)) continue;  // uniform over the block
         const float *zp = Z + (size_t)p * (size_t)ldz;
         for (int i = tid; i < m; i += kCorrThreads) zs[i] = zp[i];
         __syncthreads();
-        double *xp = X + (size_t)p * (size_t)ldx;
+        float *dxp = DX + (size_t)p * (size_t)ldx;
         for (int j = tid; j < n; j += kCorrThreads) {
-            double dl = 0.0;
+            float dl = 0.0f;
             const int q1 = __ldg(cp + j + 1);
-            for (int q = __ldg(cp + j); q < q1; ++q) dl = fma(__ldg(cv + q), (double)zs[__ldg(ri + q)], dl);
-            const double xv = xp[j] - dl;
-            xp[j] = xv;
-            xsm[j] = xv;
+            for (int q = __ldg(cp + j); q < q1; ++q) dl = fmaf(__ldg(cv + q), zs[__ldg(ri + q)], dl);
+            ds[j] = dl;
+            dxp[j] = pass == 0 ? dl : dxp[j] + dl;
         }
         __syncthreads();
+        float *rp_ = Rf + (size_t)p * (size_t)ldz;
         __nv_bfloat16 *rh = Rh + (size_t)p * (size_t)kpad, *rl = Rl + (size_t)p * (size_t)kpad;
-        unsigned long long mx = 0;
+        float mx = 0.0f, m0 = 0.0f;
         for (int i = tid; i < m; i += kCorrThreads) {
-            double acc = 0.0;
+            const float ro = rp_[i];
+            float acc = 0.0f;
             const int q1 = __ldg(rp + i + 1);
-            for (int q = __ldg(rp + i); q < q1; ++q) acc = fma(__ldg(rv + q), xsm[__ldg(ci + q)], acc);
-            mx = max(mx, (unsigned long long)__double_as_longlong(acc) & 0x7FFFFFFFFFFFFFFFull);
+            for (int q = __ldg(rp + i); q < q1; ++q) acc = fmaf(__ldg(rv + q), ds[__ldg(ci + q)], acc);
+            const float rn = ro - acc;
+            rp_[i] = rn;
+            m0 = fmaxf(m0, fabsf(ro));
+            mx = fmaxf(mx, fabsf(rn));
             if (!last) {
-                const __nv_bfloat16 hi = __double2bfloat16(acc);
+                const __nv_bfloat16 hi = __float2bfloat16_rn(rn);
                 rh[i] = hi;
-                rl[i] = __double2bfloat16(acc - (double)__bfloat162float(hi));
+                rl[i] = __float2bfloat16_rn(rn - __bfloat162float(hi));
             }
         }
 #pragma unroll
-        for (int o = 16; o; o >>= 1) mx = max(mx, (unsigned long long)__shfl_xor_sync(0xffffffffu, mx, o));
-        if (lane == 0) wmax[warp] = mx;
+        for (int o = 16; o; o >>= 1) {
+            mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+            m0 = fmaxf(m0, __shfl_xor_sync(0xffffffffu, m0, o));
+        }
+        if (lane == 0) {
+            wmax[warp][0] = mx;
+            wmax[warp][1] = m0;
+        }
         __syncthreads();
         if (tid == 0) {
-            for (int w = 1; w < kCorrThreads / 32; ++w) mx = max(mx, wmax[w]);
-            if (mx <= fine_bits) {
+            for (int w = 1; w < kCorrThreads / 32; ++w) {
+                mx = fmaxf(mx, wmax[w][0]);
+                m0 = fmaxf(m0, wmax[w][1]);
+            }
+            if (pass == 0) r0[p] = m0;  // the residual the chain's check found
+            const float target = fmaxf(fine_tol, 1e-5f * (pass == 0 ? m0 : r0[p]));
+            if (mx <= target) {
                 flags[p] &= ~SEG_REPROJ;  // converged
             } else if (!last) {
                 if (*next_any == 0ull) atomicOr(next_any, 1ull);
-            } else if (mx > tol_bits) {
+            } else if (mx > residual_tol) {
                 atomicOr(counters + CNT_ERROR, (unsigned long long)ERR_DEFER_DIVERGED);
             }
         }
@@ -159,6 +189,13 @@ achr_status ensure_defer(achr_ctx *ctx, int chains, int segments) {
         D->ld = (ctx->n + 1) & ~1;
         D->ldz = (ctx->m + 3) & ~3;
         DEFER_TRY(D->row_orig.upload(ctx->h_row_order.data(), ctx->h_row_order.size()));
+        const long long nnz = (long long)R.cv.count;
+        DEFER_TRY(D->cv32.alloc((size_t)nnz));
+        DEFER_TRY(D->rv32.alloc((size_t)nnz));
+        to_f32_kernel<<<(unsigned)((nnz + 255) / 256), 256>>>(nnz, R.cv.p, D->cv32.p);
+        to_f32_kernel<<<(unsigned)((nnz + 255) / 256), 256>>>(nnz, R.rv.p, D->rv32.p);
+        DEFER_TRY(cudaGetLastError());
+        DEFER_TRY(cudaDeviceSynchronize());
     }
     if (D->cap < chains) {
         D->cap = 0;
@@ -172,6 +209,9 @@ achr_status ensure_defer(achr_ctx *ctx, int chains, int segments) {
         DEFER_TRY(cudaMemset(D->Rh.p, 0, sizeof(unsigned short) * c * (size_t)D->kpad));
         DEFER_TRY(cudaMemset(D->Rl.p, 0, sizeof(unsigned short) * c * (size_t)D->kpad));
         DEFER_TRY(D->Z.alloc(c * (size_t)D->ldz));
+        DEFER_TRY(D->r.alloc(c * (size_t)D->ldz));
+        DEFER_TRY(D->dx.alloc(c * (size_t)D->ld));
+        DEFER_TRY(D->r0.alloc(c));
         D->cap = chains;
     }
     if (D->any_cap < segments) {
@@ -212,17 +252,17 @@ achr_status defer_sample(achr_ctx *ctx, const ChainArgs &a_in, int threads_per_c
     DeferState &D = *ctx->defer;
     const ReprojState &R = *ctx->reproj;
     const int passes = ctx->opt.reprojection_passes > 0 ? ctx->opt.reprojection_passes : kMaxPasses;
-    // A chain's pass sequence ends once max|S x| <= residual_tol / 100: the point is then within
-    // about that over the smallest singular value of S of the FP64 projection.
+    // A chain's passes end once max|S x| <= max(residual_tol / 100, 1e-5 of the residual its check
+    // found): the point is then within about that over the smallest singular value of S of the
+    // FP64 projection, i.e. within 1e-5 of the correction's own size.
     const double fine_tol = ctx->opt.residual_tol * 0.01;
 
     int dev = 0, sms = 0, per_sm = 0;
     DEFER_TRY(cudaGetDevice(&dev));
     DEFER_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    const size_t corr_smem = sizeof(double) * (size_t)D.ld + sizeof(float) * (size_t)D.ldz;
-    DEFER_TRY(cudaFuncSetAttribute(defer_correct_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)corr_smem));
-    DEFER_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, defer_correct_kernel, kCorrThreads, corr_smem));
+    const size_t corr_smem = sizeof(float) * ((size_t)D.ldz + (size_t)D.ld);
+    DEFER_TRY(cudaFuncSetAttribute(defer_pass_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)corr_smem));
+    DEFER_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, defer_pass_kernel, kCorrThreads, corr_smem));
     if (per_sm < 1) return set_err(ACHR_ERR_UNSUPPORTED, "model too large for the batched reprojection's update");
 
     ctx->last_segments = 0;
@@ -247,6 +287,9 @@ achr_status defer_sample(achr_ctx *ctx, const ChainArgs &a_in, int threads_per_c
         a.seg_Rh = D.Rh.p;
         a.seg_Rl = D.Rl.p;
         a.kpad = D.kpad;
+        a.seg_r = D.r.p;
+        a.ld_r = D.ldz;
+        a.seg_dx = D.dx.p;
         const int corr_grid = (int)std::min<long long>((long long)sms * per_sm, pc);
         int s0 = S0, seg = 0;
         for (;;) {
@@ -269,10 +312,10 @@ achr_status defer_sample(achr_ctx *ctx, const ChainArgs &a_in, int threads_per_c
                 g.gate_max = 0;
                 if (const char *why = tc_gemm_check(g)) return set_err(ACHR_ERR_INVALID, why);
                 DEFER_TRY(launch_tc_gemm(g, a_in.counters + CNT_ERROR, s));
-                defer_correct_kernel<<<(unsigned)corr_grid, kCorrThreads, corr_smem, s>>>(
-                    ctx->n, ctx->m, R.kpad, pc, D.x.p, D.ld, D.flags.p, D.Z.p, D.ldz, R.cp.p, R.ri.p, R.cv.p, R.rp.p,
-                    R.ci.p, R.rv.p, reinterpret_cast<__nv_bfloat16 *>(D.Rh.p),
-                    reinterpret_cast<__nv_bfloat16 *>(D.Rl.p), fine_tol, ctx->opt.residual_tol,
+                defer_pass_kernel<<<(unsigned)corr_grid, kCorrThreads, corr_smem, s>>>(
+                    ctx->n, ctx->m, R.kpad, pc, pass, D.flags.p, D.Z.p, D.r.p, D.ldz, D.dx.p, D.ld, D.r0.p, R.cp.p,
+                    R.ri.p, D.cv32.p, R.rp.p, R.ci.p, D.rv32.p, reinterpret_cast<__nv_bfloat16 *>(D.Rh.p),
+                    reinterpret_cast<__nv_bfloat16 *>(D.Rl.p), (float)fine_tol, (float)ctx->opt.residual_tol,
                     pass + 1 == passes ? 1 : 0, gate + pass + 1, a_in.counters);
                 DEFER_TRY(cudaGetLastError());
             }

@@ -97,6 +97,9 @@ struct ChainArgs {
     const int *row_orig;           // device row q of S -> row in the model's order
     unsigned short *seg_Rh, *seg_Rl;  // P x kpad BF16 bits: hi and lo parts of S x
     int kpad;
+    float *seg_r;                  // P x ld_r: S x in FP32 (the batched passes track it from here)
+    long long ld_r;
+    const float *seg_dx;           // P x ld_seg: the batched passes' correction, subtracted at the next launch
 };
 
 // Per-chain state bits of segmented sampling.
@@ -105,7 +108,8 @@ enum SegFlag : unsigned {
     SEG_ACCEPTED = 2u,  // at least one step accepted
     SEG_STUCK = 4u,     // stopped after max_attempts rejections
     SEG_PENDING = 8u,   // the last launch ended after a check step's update: clip and add to the centre next
-    SEG_REPROJ = 16u,   // that check found max|S x| > residual_tol: the batched pass reprojects the point
+    SEG_REPROJ = 16u,   // that check found max|S x| > residual_tol: the batched passes reproject the point
+    SEG_CORR = 32u,     // the next launch subtracts the passes' accumulated correction from the point
 };
 
 // FP32 rounding of a double toward +inf / -inf (host side).

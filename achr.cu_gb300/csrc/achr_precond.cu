@@ -302,6 +302,16 @@ __global__ void ppca_init_kernel(int d, int r, const double *__restrict__ V, con
     if (t < d) s[t] = (float)(0.5 * log(sigma2));
 }
 
+// Square root of a covariance from its eigenpairs (lam ascending, V column-major):
+// Y (d x d, row-major) = V diag(sqrt(max(lam, 0) * d)), so Y Y^T / d = V diag(lam) V^T.
+__global__ void cov_sqrt_kernel(int d, const double *__restrict__ V, const double *__restrict__ lam,
+                                float *__restrict__ Y) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)d * d) return;
+    const int i = (int)(t / d), k = (int)(t % d);
+    Y[t] = (float)(V[(long long)k * d + i] * sqrt(fmax(lam[k], 0.0) * (double)d));
+}
+
 // Standard normal (Box-Muller on two 32-bit Philox words) for entry (row, col).
 __device__ __forceinline__ float philox_normal(unsigned long long seed, unsigned row, unsigned col, unsigned tag) {
     const Philox4 w = philox4x32_10(row, col, tag, 0x6e6f726du, (uint32_t)seed, (uint32_t)(seed >> 32));
@@ -533,6 +543,7 @@ void achr_precond_default_options(achr_precond_options *opt) {
     opt->seed = 1;
     opt->init = 1;
     opt->standardize = 1;
+    opt->full_batch = 1;
 }
 
 achr_status achr_precond_loss_grad(int32_t d, int32_t r, int32_t B, const float *d_s, const float *d_U,
@@ -560,11 +571,14 @@ achr_status achr_precond_train(int32_t d, int32_t r, int32_t n_samples, const fl
                                achr_precond_stats *stats) {
     using namespace achr;
     if (!opt || d <= 0 || r <= 0 || r > 1024 || !d_Y || !d_s || !d_U || n_samples <= 0 || ldy < n_samples ||
-        opt->batch <= 0 || opt->batch > n_samples || opt->iterations < 0)
+        (!opt->full_batch && (opt->batch <= 0 || opt->batch > n_samples)) || opt->iterations < 0 ||
+        (opt->full_batch != 0 && opt->full_batch != 1))
         return pc_err(ACHR_ERR_INVALID, "bad preconditioner training arguments");
     if (opt->init && r >= d) return pc_err(ACHR_ERR_INVALID, "the PCA start needs rank < d");
     cudaStream_t st = (cudaStream_t)stream;
-    const int B = opt->batch;
+    const bool full = opt->full_batch != 0;
+    const int B = full ? d : opt->batch;
+    DevBuf<float> Yfull;  // full_batch: d columns with the samples' covariance
     // Standardised coordinates: every coordinate scaled to unit RMS, so one
     // learning rate suits coordinates whose spreads differ by orders of magnitude.
     DevBuf<float> sig, Ys;
@@ -583,7 +597,7 @@ achr_status achr_precond_train(int32_t d, int32_t r, int32_t n_samples, const fl
             ldt = n_samples;
         }
     }
-    if (opt->init) {
+    if (opt->init || full) {
         // sample covariance of the (standardised) samples, its eigenpairs in FP64
         DevBuf<float> Sig;
         DevBuf<double> Sd, lam, work;
@@ -615,13 +629,22 @@ achr_status achr_precond_train(int32_t d, int32_t r, int32_t n_samples, const fl
         std::vector<double> hl((size_t)d);
         PC_TRY(cudaMemcpyAsync(hl.data(), lam.p, sizeof(double) * d, cudaMemcpyDeviceToHost, st));
         PC_TRY(cudaStreamSynchronize(st));
-        double sigma2 = 0.0;
-        for (int k = 0; k < d - r; ++k) sigma2 += std::max(hl[(size_t)k], 0.0);
-        sigma2 = std::max(sigma2 / (double)(d - r), 1e-12 * std::max(hl.back(), 1e-300));
-        ppca_init_kernel<<<blocks_for((long long)d * r), 256, 0, st>>>(d, r, Sd.p, lam.p, sigma2, d_s, d_U);
-        PC_TRY(cudaGetLastError());
-        if (!opt->standardize)  // the start is in standardised units: bring it back
-            rescale_params_kernel<<<blocks_for((long long)d * r), 256, 0, st>>>(d, r, sig.p, d_s, d_U, 0);
+        if (full) {  // the training data from here on: the covariance's square root
+            PC_TRY(Yfull.alloc((size_t)d * d));
+            cov_sqrt_kernel<<<blocks_for((long long)d * d), 256, 0, st>>>(d, Sd.p, lam.p, Yfull.p);
+            PC_TRY(cudaGetLastError());
+        }
+        if (opt->init) {
+            double sigma2 = 0.0;
+            for (int k = 0; k < d - r; ++k) sigma2 += std::max(hl[(size_t)k], 0.0);
+            sigma2 = std::max(sigma2 / (double)(d - r), 1e-12 * std::max(hl.back(), 1e-300));
+            ppca_init_kernel<<<blocks_for((long long)d * r), 256, 0, st>>>(d, r, Sd.p, lam.p, sigma2, d_s, d_U);
+            PC_TRY(cudaGetLastError());
+            if (!opt->standardize)  // the start is in standardised units: bring it back
+                rescale_params_kernel<<<blocks_for((long long)d * r), 256, 0, st>>>(d, r, sig.p, d_s, d_U, 0);
+        } else if (opt->standardize) {
+            rescale_params_kernel<<<blocks_for((long long)d * r), 256, 0, st>>>(d, r, sig.p, d_s, d_U, 1);
+        }
     } else if (opt->standardize) {
         rescale_params_kernel<<<blocks_for((long long)d * r), 256, 0, st>>>(d, r, sig.p, d_s, d_U, 1);
     }
@@ -652,7 +675,11 @@ achr_status achr_precond_train(int32_t d, int32_t r, int32_t n_samples, const fl
         }
     } evg{e0, e1};
     PC_TRY(cudaEventRecord(e0, st));
-    const int nb = n_samples / B;  // minibatches: consecutive blocks of B samples, visited in a seeded order
+    if (full) {
+        Yt = Yfull.p;
+        ldt = d;
+    }
+    const int nb = full ? 1 : n_samples / B;  // minibatches: consecutive blocks of B samples, in a seeded order
     std::vector<int> order((size_t)nb);
     for (int q = 0; q < nb; ++q) order[(size_t)q] = q;
     uint64_t rs = opt->seed * 6364136223846793005ull + 1442695040888963407ull;

@@ -53,6 +53,7 @@ def parse_args():
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target length of the CPU baseline sample")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-ess", action="store_true", help="skip the bounded min-ESS/s and R-hat leg")
     ap.add_argument("--ess", type=int, nargs=4, metavar=("CHAINS", "BURNIN", "SEGMENTS", "STEPS"),
                     help="min-ESS/s and max R-hat from trace snapshots: CHAINS chains, BURNIN steps, then SEGMENTS "
                          "snapshots STEPS steps apart")
@@ -71,6 +72,7 @@ def parse_args():
     ap.add_argument("--pool", type=int, default=16384)
     ap.add_argument("--start", choices=["warmup", "centre"], default="warmup",
                     help="ESS runs: chains start at random warmup points (over-dispersed, default) or at the centre")
+    ap.add_argument("--minibatch", action="store_true", help="train on minibatches instead of the full covariance")
     ap.add_argument("--refine", type=int, default=0,
                     help="re-fit the preconditioner this many times on the learned sampler's own samples")
     ap.add_argument("--large-chains", type=int, default=262_144, help="chains of the large workload")
@@ -284,6 +286,48 @@ def run_reference(args):
     return 0
 
 
+def ess_leg(pkg, synth, args, genome_inputs):
+    """The metric's second half (min-ESS/s and R-hat), bounded to about a minute of the default run.
+
+    * small 72 x 95 model: plain ACHR, isotropic hit-and-run, PCA-only and learned directions
+      (learned_study) on a schedule where the chains reach R-hat < 1.01: 1000 chains from random
+      warmup points, 100,000 burn-in steps, 200 draws 1000 steps apart; training on 65,536 chains
+      x (2000 + 8 x 250) plain steps, rank 4 (the basis has 9 directions), 2000 full-batch Adam steps.
+    * the bench's own genome model: plain ACHR, 512 chains from random warmup points, 20,000 burn-in
+      steps, 40 draws 500 steps apart (far from R-hat < 1.01 at this length; reported as measured).
+    min-ESS/s divides the smallest bulk ESS over the moving fluxes by the device time of the
+    sampling launches (burn-in included)."""
+    import importlib
+
+    import torch
+
+    diag = importlib.import_module("achr_gb300.diagnostics")
+    t0 = time.perf_counter()
+    out = {}
+    spec_s, model_s, _, warm_s, _, _ = build_inputs("small", pkg, synth, warmup_form=args.warmup_form)
+    with pkg.Sampler(model_s, warm_s) as smp:
+        res = learned_study(pkg, diag, smp, warm_s, seed=args.seed, train=(65536, 2000, 8, 250), rank=4, iters=2000,
+                            lr=0.01, batch=4096, pool=16384, schedule=(1000, 100000, 200, 1000))
+    res.pop("value")
+    out["small"] = {"model": f"{spec_s.n_mets}x{spec_s.n_rxns}", **res}
+    spec, model, warm = genome_inputs
+    M, B, K, L = 512, 20000, 40, 500
+    stream = torch.cuda.current_stream().cuda_stream
+    with pkg.Sampler(model, warm) as smp:
+        draws, ms, steps = ess_trace(smp, M, B, K, L, args.seed + 101, stream,
+                                     starts=dispersed_starts(warm, M, args.seed + 5))
+    summ = diag.summarize(draws, exclude=pinned_reactions(warm))
+    out["genome_plain"] = {"model": f"{spec.n_mets}x{spec.n_rxns}",
+                           "schedule": {"chains": M, "burnin": B, "draws": K, "gap": L,
+                                        "starts": "random warmup points"},
+                           "min_ess_per_s": summ["min_ess"] / (ms * 1e-3), "min_ess": summ["min_ess"],
+                           "max_rhat": summ["max_rhat"], "rhat_below_1.01": summ["max_rhat"] < 1.01,
+                           "median_rhat": summ["median_rhat"], "sampling_ms": ms,
+                           "chain_steps_per_s": steps / (ms * 1e-3)}
+    out["seconds"] = time.perf_counter() - t0
+    return out
+
+
 def run_gpu(args):
     rank, world, local = dist_info()
     import torch
@@ -379,6 +423,10 @@ def run_gpu(args):
         Nb = smp.null_space()
         cpu = cpu_baseline(oracle, model, warm, Nb, T, args.seed, args.cpu_seconds)
 
+    ess = None
+    if rank == 0 and world == 1 and not args.no_ess:
+        ess = ess_leg(pkg, synth, args, (spec, model, warm))
+
     line = {
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
@@ -393,9 +441,11 @@ def run_gpu(args):
         "cpu_baseline": cpu,
         "e2e": e2e,
         "clocks": clk,
+        "ess": ess,
         "sampler": {"null_dim": smp.null_dim, "setup_s": setup_s,
                     **({k: stats[k] for k in ("accepted", "rejected", "checks", "reprojections", "stuck_chains",
-                                              "exact_evals", "max_residual", "max_bound_violation")} if stats else {})},
+                                              "exact_evals", "max_residual", "max_bound_violation", "segments")}
+                       if stats else {})},
     }
     if rank == 0:
         print(json.dumps(line), flush=True)
@@ -620,26 +670,113 @@ def run_ess(args):
     return 0
 
 
-def run_learned(args):
-    """Learned-preconditioned hit-and-run against plain ACHR, by min-ESS/s.
-
-    1. Plain ACHR (reference semantics) from the warmup centre: TRAIN_CHAINS
-       chains, TRAIN_BURNIN steps, then TRAIN_SNAPSHOTS snapshots TRAIN_GAP steps
-       apart; every snapshot goes to null-space coordinates on the tensor cores
-       (achr_null_coords) and is centred.
-    2. The low-rank (--precond-rank) plus diagonal map is fitted to those samples by the
-       Gaussian KL loss with Adam (achr_precond_train, --iters steps).
-    3. A pool of --pool directions B L z (B: the basis of the directions the
-       polytope spans) is installed (achr_precond_pool); the sampler then runs
-       hit-and-run.
-       With --refine R the fit is repeated R times on samples of the learned
-       sampler itself (same schedule, fresh chain ids).
-    4. Both samplers run the same ESS schedule (--learned CHAINS BURNIN SEGMENTS
-       STEPS, fresh chains from the warmup centre, another seed); min-ESS/s
-       counts the device time of the sampling launches.  If the learned
-       sampler's max R-hat is not below 1.01 while plain ACHR's is, the
-       reported value falls back to plain ACHR's."""
+def training_samples(smp, d, seed, train, chain_offset=0):
+    """Centred samples of the context's current sampler in the preconditioner's coordinates
+    (d x P*K, FP32, device): P chains, Tb burn-in steps, then K snapshots Lg steps apart, each
+    mapped by achr_null_coords on the tensor cores.  Returns (Y, device ms of the sampling)."""
     import torch
+
+    n = smp.n
+    Pt, Tb, Ks, Lg = train
+    stream = torch.cuda.current_stream().cuda_stream
+    x = torch.zeros((n, Pt), dtype=torch.float64, device="cuda")
+    a = torch.zeros_like(x)
+    mu = torch.from_numpy(smp.centre()).cuda()
+    Y = torch.empty((d, Pt * Ks), dtype=torch.float32, device="cuda")
+    st = smp.sample_resume(Pt, 0, Tb, False, x.data_ptr(), a.data_ptr(), Pt, stream=stream, seed=seed,
+                           chain_offset=chain_offset, with_stats=True)
+    gen_ms = st["kernel_ms"]
+    for k in range(Ks):
+        st = smp.sample_resume(Pt, Tb + k * Lg, Lg, True, x.data_ptr(), a.data_ptr(), Pt, stream=stream, seed=seed,
+                               chain_offset=chain_offset, with_stats=True)
+        gen_ms += st["kernel_ms"]
+        smp.null_coords(Pt, x.data_ptr(), Pt, Y.data_ptr() + 4 * k * Pt, Pt * Ks, d_mu=mu.data_ptr(), stream=stream)
+    del x, a
+    Y -= Y.mean(dim=1, keepdim=True)
+    return Y, gen_ms
+
+
+def learned_study(pkg, diag, smp, warm, *, seed, train, rank, iters, lr, batch, pool, schedule, start="warmup",
+                  refine=0, full_batch=1):
+    """Plain ACHR against hit-and-run along learned directions, with the two ablations that
+    isolate the learning, all on one ESS schedule (same chains, same starts, same seed):
+
+      plain      ACHR, the reference's direction law (warmup point minus centre)
+      isotropic  hit-and-run along B z, z ~ N(0, I): the preconditioner's basis, no fit
+      pca        hit-and-run along the probabilistic-PCA fit of the samples (no Adam)
+      learned    hit-and-run along the map trained from that start (achr_precond_train)
+
+    B is the basis of the directions the polytope spans (pinned reactions held fixed).
+    Returns a dict of per-sampler min-ESS/s, R-hat and rates, the training record and the
+    fallback decision (learned not below R-hat 1.01 while plain is)."""
+    import torch
+
+    stream = torch.cuda.current_stream().cuda_stream
+    d, n_frozen = smp.precond_dim()
+    r = min(rank, max(1, d - 1))
+    t0 = time.perf_counter()
+    Y, gen_ms = training_samples(smp, d, seed + 7, train)
+    ns = Y.shape[1]
+    s_pca = torch.zeros(d, dtype=torch.float32, device="cuda")
+    U_pca = torch.zeros((d, r), dtype=torch.float32, device="cuda")
+    pkg.precond_train(d, r, ns, Y.data_ptr(), ns, s_pca.data_ptr(), U_pca.data_ptr(), stream=stream, iterations=0,
+                      batch=min(batch, ns), init=1)
+    s_par, U_par = s_pca.clone(), U_pca.clone()
+    tst = pkg.precond_train(d, r, ns, Y.data_ptr(), ns, s_par.data_ptr(), U_par.data_ptr(), stream=stream,
+                            iterations=iters, batch=min(batch, ns), learning_rate=lr, seed=seed, init=1,
+                            full_batch=full_batch)
+    refine_rec = []
+    for rnd in range(refine):  # re-fit on samples of the learned sampler itself (fresh chain ids)
+        smp.precond_pool(r, s_par.data_ptr(), U_par.data_ptr(), pool, seed=seed + 11)
+        Y, _ = training_samples(smp, d, seed + 7, train, chain_offset=(rnd + 1) * train[0])
+        smp.set_directions(None)
+        refine_rec.append(pkg.precond_train(d, r, ns, Y.data_ptr(), ns, s_par.data_ptr(), U_par.data_ptr(),
+                                            stream=stream, iterations=iters, batch=min(batch, ns),
+                                            learning_rate=lr, seed=seed + rnd + 1, init=0, full_batch=full_batch))
+    del Y
+    torch.cuda.empty_cache()
+    train_s = time.perf_counter() - t0
+    s_iso = torch.zeros(d, dtype=torch.float32, device="cuda")
+    U_iso = torch.zeros((d, r), dtype=torch.float32, device="cuda")
+    M, B, K, L = schedule
+    starts = dispersed_starts(warm, M, seed + 5) if start == "warmup" else None
+    out = {}
+    for name, pars in (("plain", None), ("isotropic", (s_iso, U_iso)), ("pca", (s_pca, U_pca)),
+                       ("learned", (s_par, U_par))):
+        if pars is None:
+            smp.set_directions(None)
+        else:
+            smp.precond_pool(r, pars[0].data_ptr(), pars[1].data_ptr(), pool, seed=seed + 11)
+        draws, ms, steps = ess_trace(smp, M, B, K, L, seed + 101, stream, starts=starts)
+        summ = diag.summarize(draws, exclude=pinned_reactions(warm))
+        out[name] = {"min_ess_per_s": summ["min_ess"] / (ms * 1e-3), "min_ess": summ["min_ess"],
+                     "max_rhat": summ["max_rhat"], "median_rhat": summ["median_rhat"],
+                     "rhat_q99": summ["rhat_q99"], "median_ess": summ["median_ess"], "sampling_ms": ms,
+                     "chain_steps_per_s": steps / (ms * 1e-3), "frozen_fluxes": summ["frozen_params"]}
+    smp.set_directions(None)
+    lp, ll = out["plain"], out["learned"]
+    fallback = ll["max_rhat"] >= 1.01 and lp["max_rhat"] < 1.01
+    return {
+        **out,
+        "learned_over_plain": ll["min_ess_per_s"] / lp["min_ess_per_s"],
+        "learned_over_isotropic": ll["min_ess_per_s"] / out["isotropic"]["min_ess_per_s"],
+        "learned_over_pca": ll["min_ess_per_s"] / out["pca"]["min_ess_per_s"],
+        "fallback_to_plain": fallback,
+        "value": lp["min_ess_per_s"] if fallback else ll["min_ess_per_s"],
+        "schedule": {"chains": M, "burnin": B, "draws": K, "gap": L,
+                     "starts": "random warmup points" if start == "warmup" else "the warmup centre"},
+        "training": {"samples": ns, "basis_dim": d, "rank": r, "null_dim": smp.null_dim, "pinned_reactions": n_frozen,
+                     "generation_ms": gen_ms, "full_batch": bool(full_batch), **tst, "refine_rounds": refine_rec,
+                     "total_s": train_s},
+    }
+
+
+def run_learned(args):
+    """Learned-preconditioned hit-and-run against plain ACHR, by min-ESS/s (see learned_study):
+    training on --train-chains x (--train-burnin + --train-snapshots x --train-gap) plain-ACHR
+    steps, --iters Adam steps (full batch unless --minibatch), a pool of --pool directions, then the
+    ESS schedule --learned CHAINS BURNIN SEGMENTS STEPS for plain, isotropic, PCA-only and learned."""
+    import torch  # noqa: F401
 
     import __graft_entry__ as ge
 
@@ -649,96 +786,28 @@ def run_learned(args):
     synth = importlib.import_module("achr_gb300.synthetic")
     diag = importlib.import_module("achr_gb300.diagnostics")
     t_setup = time.perf_counter()
-    spec, model, S, warm, _, _ = build_inputs(args.workload, pkg, synth, null_space=gpu_null_space_fn(pkg))
-    n = spec.n_rxns
-    stream = torch.cuda.current_stream().cuda_stream
-    plain = pkg.Sampler(model, warm)
-    tpc = plain.autotune()
-    d, n_frozen = plain.precond_dim()  # directions the polytope spans (pinned reactions held fixed)
-    null_dim = plain.null_dim
+    spec, model, S, warm, _, _ = build_inputs(args.workload, pkg, synth, null_space=gpu_null_space_fn(pkg),
+                                              warmup_form=args.warmup_form)
+    smp = pkg.Sampler(model, warm)
+    tpc = smp.autotune()
     setup_s = time.perf_counter() - t_setup
-
-    # 1. training samples
-    Pt, Tb, Ks, Lg = args.train_chains, args.train_burnin, args.train_snapshots, args.train_gap
-    t_train = time.perf_counter()
-    x = torch.zeros((n, Pt), dtype=torch.float64, device="cuda")
-    a = torch.zeros_like(x)
-    mu = torch.from_numpy(plain.centre()).cuda()
-    Y = torch.empty((d, Pt * Ks), dtype=torch.float32, device="cuda")
-    st = plain.sample_resume(Pt, 0, Tb, False, x.data_ptr(), a.data_ptr(), Pt, stream=stream, seed=args.seed + 7,
-                             with_stats=True)
-    gen_ms = st["kernel_ms"]
-    for k in range(Ks):
-        st = plain.sample_resume(Pt, Tb + k * Lg, Lg, True, x.data_ptr(), a.data_ptr(), Pt, stream=stream,
-                                 seed=args.seed + 7, with_stats=True)
-        gen_ms += st["kernel_ms"]
-        plain.null_coords(Pt, x.data_ptr(), Pt, Y.data_ptr() + 4 * k * Pt, Pt * Ks, d_mu=mu.data_ptr(),
-                          stream=stream)
-    del x, a
-    Y -= Y.mean(dim=1, keepdim=True)
-    # start: the probabilistic-PCA fit of the samples (computed by the library)
-    s_par = torch.zeros(d, dtype=torch.float32, device="cuda")
-    U_par = torch.zeros((d, args.precond_rank), dtype=torch.float32, device="cuda")
-    tst = pkg.precond_train(d, args.precond_rank, Pt * Ks, Y.data_ptr(), Pt * Ks, s_par.data_ptr(), U_par.data_ptr(),
-                            stream=stream, iterations=args.iters, batch=args.batch, learning_rate=args.lr,
-                            seed=args.seed)
-    refine = []
-    for rnd in range(args.refine):
-        # re-fit on samples of the learned sampler itself (same schedule, fresh chain ids)
-        plain.precond_pool(args.precond_rank, s_par.data_ptr(), U_par.data_ptr(), args.pool, seed=args.seed + 11)
-        x = torch.zeros((n, Pt), dtype=torch.float64, device="cuda")
-        a = torch.zeros_like(x)
-        off = (rnd + 1) * Pt
-        st = plain.sample_resume(Pt, 0, Tb, False, x.data_ptr(), a.data_ptr(), Pt, stream=stream,
-                                 seed=args.seed + 7, chain_offset=off, with_stats=True)
-        for k in range(Ks):
-            plain.sample_resume(Pt, Tb + k * Lg, Lg, True, x.data_ptr(), a.data_ptr(), Pt, stream=stream,
-                                seed=args.seed + 7, chain_offset=off)
-            plain.null_coords(Pt, x.data_ptr(), Pt, Y.data_ptr() + 4 * k * Pt, Pt * Ks, d_mu=mu.data_ptr(),
-                              stream=stream)
-        del x, a
-        plain.set_directions(None)
-        Y -= Y.mean(dim=1, keepdim=True)
-        refine.append(pkg.precond_train(d, args.precond_rank, Pt * Ks, Y.data_ptr(), Pt * Ks, s_par.data_ptr(),
-                                        U_par.data_ptr(), stream=stream, iterations=args.iters, batch=args.batch,
-                                        learning_rate=args.lr, seed=args.seed + rnd + 1))
-    del Y
-    torch.cuda.empty_cache()
-    train_s = time.perf_counter() - t_train
-
-    # 4. ESS comparison on the same schedule; the same context switches to the
-    # learned pool after the plain run, so both use the same basis.
+    res = learned_study(pkg, diag, smp, warm, seed=args.seed,
+                        train=(args.train_chains, args.train_burnin, args.train_snapshots, args.train_gap),
+                        rank=args.precond_rank, iters=args.iters, lr=args.lr, batch=args.batch, pool=args.pool,
+                        schedule=tuple(args.learned), start=args.start, refine=args.refine,
+                        full_batch=0 if args.minibatch else 1)
     M, B, K, L = args.learned
-    starts = dispersed_starts(warm, M, args.seed + 5) if args.start == "warmup" else None
-    out = {}
-    for name in ("plain", "learned"):
-        if name == "learned":
-            plain.precond_pool(args.precond_rank, s_par.data_ptr(), U_par.data_ptr(), args.pool, seed=args.seed + 11)
-        draws, ms, steps = ess_trace(plain, M, B, K, L, args.seed + 101, stream, starts=starts)
-        summ = diag.summarize(draws, exclude=pinned_reactions(warm))
-        out[name] = {"min_ess_per_s": summ["min_ess"] / (ms * 1e-3), "min_ess": summ["min_ess"],
-                     "max_rhat": summ["max_rhat"], "median_rhat": summ["median_rhat"],
-                     "rhat_q99": summ["rhat_q99"], "median_ess": summ["median_ess"], "sampling_ms": ms,
-                     "chain_steps_per_s": steps / (ms * 1e-3), "frozen_fluxes": summ["frozen_params"]}
-    lp, ll = out["plain"], out["learned"]
-    fallback = ll["max_rhat"] >= 1.01 and lp["max_rhat"] < 1.01
     line = {
-        "metric": "min-ESS/s", "value": lp["min_ess_per_s"] if fallback else ll["min_ess_per_s"],
-        "unit": "effective samples/s", "higher_is_better": True, "n_gpus": 1, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"{args.workload}: {spec.n_mets}x{n}, {M} chains, {B} burn-in steps, {K} draws {L} "
-                               f"steps apart, chains start at "
-                               f"{'random warmup points' if args.start == 'warmup' else 'the warmup centre'}; "
-                               f"learned: rank {args.precond_rank} + diagonal, {args.iters} Adam steps on "
-                               f"{Pt * Ks} plain-ACHR samples, pool of {args.pool} directions",
+        "metric": "min-ESS/s", "value": res.pop("value"), "unit": "effective samples/s", "higher_is_better": True,
+        "n_gpus": 1, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"{args.workload}: {spec.n_mets}x{spec.n_rxns}, {M} chains, {B} burn-in steps, {K} "
+                               f"draws {L} steps apart, warmups {args.warmup_form}; learned: rank "
+                               f"{res['training']['rank']} + diagonal, {args.iters} Adam steps",
                    "threads_per_chain": tpc},
-        "learned_over_plain": ll["min_ess_per_s"] / lp["min_ess_per_s"], "fallback_to_plain": fallback,
-        "plain": lp, "learned": ll,
-        "training": {"samples": Pt * Ks, "basis_dim": d, "null_dim": null_dim, "pinned_reactions": n_frozen,
-                     "generation_ms": gen_ms, **tst, "refine_rounds": refine, "total_s": train_s},
-        "setup_s": setup_s,
+        **res, "setup_s": setup_s,
     }
     print(json.dumps(line), flush=True)
-    plain.close()
+    smp.close()
     return 0
 
 

@@ -229,11 +229,16 @@ typedef struct achr_precond_options {
     int32_t init;          /* 1: start from the probabilistic-PCA fit of the samples (overwrites s, U);
                               0: start from the s, U passed in */
     int32_t standardize;   /* 1: train in coordinates scaled to unit RMS (results returned unscaled) */
+    int32_t full_batch;    /* 1 (default): every step's loss and gradients are those of all n_samples
+                              samples: the samples are replaced by d columns with the same covariance,
+                              V Lambda^1/2 sqrt(d) from its eigen-decomposition, so a step costs a d-sample
+                              minibatch and carries no sampling noise; batch and seed are then unused.
+                              0: minibatches of `batch` consecutive samples in a seeded order */
 } achr_precond_options;
 
 typedef struct achr_precond_stats {
-    double loss_first;     /* mean loss over the first 20 minibatches */
-    double loss_last;      /* mean loss over the last 20 minibatches */
+    double loss_first;     /* mean loss over the first 20 steps (the full-sample loss with full_batch) */
+    double loss_last;      /* mean loss over the last 20 steps */
     double train_ms;
     int32_t iterations;
 } achr_precond_stats;

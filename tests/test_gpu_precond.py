@@ -92,7 +92,7 @@ def test_training_fits_a_known_covariance(pkg):
     U0 = 0.01 * rng.standard_normal((d, r))
     ds, dU, dY = _dev(s0), _dev(U0), _dev(Y)
     st = pkg.precond_train(d, r, n, dY.data_ptr(), n, ds.data_ptr(), dU.data_ptr(), iterations=1500, batch=2048,
-                           learning_rate=0.02)
+                           learning_rate=0.02, init=0, full_batch=0)
     assert st["iterations"] == 1500 and st["loss_last"] < st["loss_first"]
     s_fit, U_fit = ds.cpu().numpy().astype(np.float64), dU.cpu().numpy().astype(np.float64)
     kl_fit = precond.kl_to_sample_covariance(s_fit, U_fit, Y)
@@ -100,6 +100,34 @@ def test_training_fits_a_known_covariance(pkg):
     kl_true = precond.kl_to_sample_covariance(s_true, U_true, Y)
     # minibatch noise keeps Adam near, not at, the optimum
     assert kl_fit < 0.05 * kl_init and kl_fit < kl_true + 0.2
+
+
+def test_full_batch_training_reaches_the_optimum(pkg):
+    """Full-batch steps (the samples replaced by their covariance's square root): from the
+    probabilistic-PCA start the exact loss falls, and the fit ends at least as close to the sample
+    covariance as the true parameters (which lie in the model family) and closer than the start."""
+    from oracle import precond
+    rng = np.random.default_rng(6)
+    d, r, n = 64, 4, 32768
+    s_true = np.log(rng.uniform(0.2, 2.0, d))
+    U_true = rng.standard_normal((d, r)) * 1.5
+    Y = np.linalg.cholesky(precond.covariance(s_true, U_true)) @ rng.standard_normal((d, n))
+    ds, dU, dY = _dev(np.zeros(d)), _dev(np.zeros((d, r))), _dev(Y)
+    pkg.precond_train(d, r, n, dY.data_ptr(), n, ds.data_ptr(), dU.data_ptr(), iterations=0, init=1)
+    s_p, U_p = ds.cpu().numpy().astype(np.float64), dU.cpu().numpy().astype(np.float64)
+    st = pkg.precond_train(d, r, n, dY.data_ptr(), n, ds.data_ptr(), dU.data_ptr(), iterations=1500,
+                           learning_rate=0.01, init=1, full_batch=1)
+    s_fit, U_fit = ds.cpu().numpy().astype(np.float64), dU.cpu().numpy().astype(np.float64)
+    kl_pca = precond.kl_to_sample_covariance(s_p, U_p, Y)
+    kl_fit = precond.kl_to_sample_covariance(s_fit, U_fit, Y)
+    kl_true = precond.kl_to_sample_covariance(s_true, U_true, Y)
+    assert st["loss_last"] < st["loss_first"]
+    # the full-sample loss of the fit, from the FP64 oracle, equals what the GPU reports (training runs
+    # in coordinates scaled to unit RMS, which shifts the loss by -sum(log rms))
+    rms = np.sqrt((Y ** 2).mean(axis=1))
+    want = precond.loss(s_fit, U_fit, Y) - np.log(rms).sum()
+    assert abs(want - st["loss_last"]) <= 1e-3 * abs(want) + 1e-3, (want, st["loss_last"])
+    assert kl_fit < kl_pca and kl_fit <= kl_true + 0.01, (kl_fit, kl_pca, kl_true)
 
 
 def test_precond_basis_spans_the_affine_hull(pkg, sampler, small_model, golden):
