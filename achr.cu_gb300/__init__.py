@@ -74,7 +74,9 @@ class Stats(C.Structure):
         ("accepted", C.c_int64), ("rejected", C.c_int64), ("checks", C.c_int64), ("reprojections", C.c_int64),
         ("stuck_chains", C.c_int64), ("exact_evals", C.c_int64), ("final_projections", C.c_int64),
         ("max_residual", C.c_double), ("max_bound_violation", C.c_double), ("kernel_ms", C.c_double),
-        ("segments", C.c_int64),
+        ("segments", C.c_int64), ("reprojection_passes", C.c_int64), ("reprojection_gemms", C.c_int64),
+        ("chain_ms", C.c_double), ("reprojection_ms", C.c_double), ("reprojection_flops", C.c_double),
+        ("kernel_launches", C.c_int64),
     ]
 
     def as_dict(self) -> dict:
@@ -111,6 +113,13 @@ class ReprojStats(C.Structure):
         ("total_ms", C.c_double), ("gemm_flops", C.c_double), ("rounds", C.c_int32), ("rank", C.c_int32),
         ("lambda_min", C.c_double), ("lambda_max", C.c_double),
     ]
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+class DirectionCheck(C.Structure):
+    _fields_ = [("rhat_max", C.c_double), ("fluxes", C.c_int32), ("kept", C.c_int32), ("sampling_ms", C.c_double)]
 
     def as_dict(self) -> dict:
         return {name: getattr(self, name) for name, _ in self._fields_}
@@ -157,6 +166,8 @@ _SIGNATURES = {
     "achr_set_directions": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_int32]),
     "achr_get_n_directions": (C.c_int32, [C.c_void_p]),
     "achr_get_directions": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "achr_check_directions": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_uint64,
+                                        C.c_double, C.POINTER(DirectionCheck)]),
     "achr_precond_default_options": (None, [C.POINTER(PrecondOptions)]),
     "achr_precond_dim": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
     "achr_get_precond_basis": (C.c_int, [C.c_void_p, C.c_void_p]),
@@ -409,6 +420,13 @@ class Sampler:
         if k:
             _check(lib().achr_get_directions(self._ctx, out.ctypes.data_as(C.c_void_p)))
         return out
+
+    def check_directions(self, chains: int = 256, burnin: int = 20000, draws: int = 100, gap: int = 200,
+                         seed: int = 0, rhat_limit: float = 1.01) -> dict:
+        """Pilot of the installed pool; removes it (back to plain ACHR) when max split-R-hat >= rhat_limit."""
+        out = DirectionCheck()
+        _check(lib().achr_check_directions(self._ctx, chains, burnin, draws, gap, seed, rhat_limit, C.byref(out)))
+        return out.as_dict()
 
     def precond_dim(self) -> tuple[int, int]:
         """(dimension of the preconditioner's basis, reactions pinned across all warmup points)."""

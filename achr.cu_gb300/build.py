@@ -25,7 +25,7 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-r
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-Wall", "-Wno-unused-function"]
 
 CU_SOURCES = ["achr_chain_cfg_small.cu", "achr_chain_cfg_mid.cu", "achr_chain_cfg_large.cu", "achr_chain_launch.cu", "achr_capi.cu",
-              "achr_noalloc.cu", "achr_tc_gemm.cu", "achr_reproject.cu", "achr_defer.cu", "achr_precond.cu"]
+              "achr_noalloc.cu", "achr_tc_gemm.cu", "achr_reproject.cu", "achr_defer.cu", "achr_precond.cu", "achr_rhat.cu"]
 CXX_SOURCES = ["achr_io.cpp"]
 
 

@@ -345,6 +345,25 @@ achr_status prepare_warmup_and_centre(achr_ctx *ctx) {
 ChainArgs chain_args(const achr_ctx *ctx, uint64_t seed, uint64_t chain_offset, int32_t n_points, int32_t n_steps,
                      double *d_points_out, int64_t ld_out);
 
+achr_status read_counters(achr_ctx *ctx, achr_stats *stats, float ms);
+
+// The deferred-reprojection part of the statistics (after the stream has completed).
+achr_status deferred_stats(achr_ctx *ctx, bool deferred, achr_stats *stats) {
+    stats->chain_ms = stats->kernel_ms;
+    stats->kernel_launches = 1;
+    if (!deferred) return ACHR_OK;
+    stats->segments = ctx->last_segments;
+    stats->kernel_launches = ctx->last_launches;
+    double cm = 0.0, pm = 0.0, per_sweep = 0.0;
+    achr_status st = achr::defer_times(ctx, &cm, &pm, &per_sweep);
+    if (st != ACHR_OK) return st;
+    stats->chain_ms = cm;
+    stats->reprojection_ms = pm;
+    const int kpad = (ctx->m + 63) / 64 * 64;
+    stats->reprojection_flops = (double)stats->reprojection_gemms * 2.0 * per_sweep * ctx->m * kpad * 3.0;
+    return ACHR_OK;
+}
+
 achr_status read_counters(achr_ctx *ctx, achr_stats *stats, float ms) {
     unsigned long long c[achr::CNT_SLOTS];
     ACHR_CUDA_TRY(cudaMemcpy(c, ctx->counters.p, sizeof(c), cudaMemcpyDeviceToHost));
@@ -369,6 +388,12 @@ achr_status read_counters(achr_ctx *ctx, achr_stats *stats, float ms) {
         stats->max_bound_violation = v;
         stats->kernel_ms = ms;
         stats->segments = 0;
+        stats->reprojection_passes = (int64_t)c[achr::CNT_PASSES];
+        stats->reprojection_gemms = (int64_t)c[achr::CNT_GEMMS];
+        stats->chain_ms = ms;
+        stats->reprojection_ms = 0.0;
+        stats->reprojection_flops = 0.0;
+        stats->kernel_launches = 1;
     }
     return ACHR_OK;
 }
@@ -639,7 +664,7 @@ achr_status achr_sample_device(achr_ctx *ctx, uint64_t seed, uint64_t chain_offs
     }
     cudaError_t e = cudaSuccess;
     achr_status dst = ACHR_OK;
-    if (deferred) dst = achr::defer_sample(ctx, a, ctx->opt.threads_per_chain, s);
+    if (deferred) dst = achr::defer_sample(ctx, a, ctx->opt.threads_per_chain, s, stats != nullptr);
     else e = achr::launch_chains(a, ctx->opt.threads_per_chain, s);
     if (e != cudaSuccess || dst != ACHR_OK) {
         if (e0) cudaEventDestroy(e0);
@@ -654,7 +679,7 @@ achr_status achr_sample_device(achr_ctx *ctx, uint64_t seed, uint64_t chain_offs
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     achr_status rst = read_counters(ctx, stats, ms);
-    if (rst == ACHR_OK) stats->segments = deferred ? ctx->last_segments : 0;
+    if (rst == ACHR_OK) rst = deferred_stats(ctx, deferred, stats);
     return rst;
 }
 
@@ -807,7 +832,7 @@ achr_status achr_sample_resume(achr_ctx *ctx, uint64_t seed, uint64_t chain_offs
     const bool deferred = achr::defer_selected(ctx) && n_points > 0 && n_steps > 0;
     cudaError_t e = cudaSuccess;
     achr_status dst = ACHR_OK;
-    if (deferred) dst = achr::defer_sample(ctx, a, ctx->opt.threads_per_chain, s);
+    if (deferred) dst = achr::defer_sample(ctx, a, ctx->opt.threads_per_chain, s, stats != nullptr);
     else e = achr::launch_chains(a, ctx->opt.threads_per_chain, s);
     if (e != cudaSuccess || dst != ACHR_OK) {
         if (e0) cudaEventDestroy(e0);
@@ -822,7 +847,7 @@ achr_status achr_sample_resume(achr_ctx *ctx, uint64_t seed, uint64_t chain_offs
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     achr_status rst = read_counters(ctx, stats, ms);
-    if (rst == ACHR_OK) stats->segments = deferred ? ctx->last_segments : 0;
+    if (rst == ACHR_OK) rst = deferred_stats(ctx, deferred, stats);
     return rst;
 }
 

@@ -441,7 +441,9 @@ __host__ __device__ inline size_t chain_smem_bytes_cfg(int np, int d, int bd) {
     return sizeof(double) * 3 * (size_t)np + sizeof(StepEntry) * kTbl + 2 * sizeof(RedSlots) + 128;
 }
 
-template <int BD, int EPT>
+// SEG: segmented launches of the deferred reprojection (a separate
+// instantiation, so the plain kernel carries none of its code or registers).
+template <int BD, int EPT, bool SEG>
 __global__ void __launch_bounds__(BD, (BD <= 384 ? 2 : 1)) achr_chain_kernel(const ChainArgs a) {
     constexpr int NP = BD * EPT;
     constexpr int NW = BD / 32;
@@ -493,7 +495,7 @@ __global__ void __launch_bounds__(BD, (BD <= 384 ? 2 : 1)) achr_chain_kernel(con
     for (int p = blockIdx.x; p < a.P && !failed; p = (int)min((long long)p + gridDim.x, (long long)a.P)) {
 #define ACHR_CHAIN_ID (a.chain_offset + (unsigned long long)p)
         // Segmented sampling: the chain's state bits from the earlier launches.
-        const unsigned sflags = a.seg ? a.seg_flags[p] : 0u;
+        const unsigned sflags = SEG ? a.seg_flags[p] : 0u;
         if (sflags & SEG_STARTED) {
 #pragma unroll
             for (int k = 0; k < EPT; ++k) {
@@ -524,8 +526,9 @@ __global__ void __launch_bounds__(BD, (BD <= 384 ? 2 : 1)) achr_chain_kernel(con
         const bool was_stuck = (sflags & SEG_STUCK) != 0;
         if (was_stuck) stuck = true;  // stopped in an earlier launch: no more steps
         if (sflags & SEG_CORR) {
-            // The batched passes' correction of this chain (x <- x - S^T z summed over
-            // the passes, in FP32: it is at most the size of the residual's preimage).
+            // The later batched passes' correction of this chain (x <- x - S^T z summed
+            // over the passes after the first, in FP32: it is what the first FP64 pass
+            // left, ~1e-4 of the residual's preimage).
 #pragma unroll
             for (int k = 0; k < EPT; ++k) {
                 const int i = tid + k * BD;
@@ -968,7 +971,7 @@ __global__ void __launch_bounds__(BD, (BD <= 384 ? 2 : 1)) achr_chain_kernel(con
                         xs[i] = xc;
                         As[i] += xc;
                     }
-                } else if (a.seg) {
+                } else if (SEG) {
                     // Segmented sampling: the check ends this launch for the chain.
 #pragma unroll
                     for (int k = 0; k < EPT; ++k) {
@@ -1021,7 +1024,7 @@ __global__ void __launch_bounds__(BD, (BD <= 384 ? 2 : 1)) achr_chain_kernel(con
                     }
                     if (tid == 0) {
                         a.seg_flags[p] =
-                            SEG_STARTED | SEG_ACCEPTED | SEG_PENDING | (reproject ? SEG_REPROJ | SEG_CORR : 0u);
+                            SEG_STARTED | SEG_ACCEPTED | SEG_PENDING | (reproject ? SEG_REPROJ : 0u);
                         ++cnt[CNT_ACCEPTED];
                     }
                     __syncthreads();  // the residual rows in ws are read before the next chain's column lands
@@ -1119,7 +1122,7 @@ __global__ void __launch_bounds__(BD, (BD <= 384 ? 2 : 1)) achr_chain_kernel(con
             failed = true;
             break;
         }
-        if (a.seg && !seg_pending && !a.seg_final) {
+        if (SEG && !seg_pending && !a.seg_final) {
             // A segmented launch that is not the run's last: keep the state for the next one.
 #pragma unroll
             for (int k = 0; k < EPT; ++k) {
@@ -1132,7 +1135,7 @@ __global__ void __launch_bounds__(BD, (BD <= 384 ? 2 : 1)) achr_chain_kernel(con
             if (tid == 0)
                 a.seg_flags[p] = SEG_STARTED | (any_accepted ? SEG_ACCEPTED : 0u) | (stuck ? SEG_STUCK : 0u);
         }
-        if (a.seg && (seg_pending || !a.seg_final)) {
+        if (SEG && (seg_pending || !a.seg_final)) {
             __syncthreads();
             continue;  // the point is emitted by the run's last launch
         }
@@ -1213,8 +1216,9 @@ __global__ void __launch_bounds__(BD, (BD <= 384 ? 2 : 1)) achr_chain_kernel(con
 // Occupancy-sized persistent launch of one configuration.  max_ctas > 0 caps
 // the grid; max_ctas < 0 launches one CTA per chain, leaving the balancing of
 // concurrent launches to the hardware CTA scheduler (batched models).
-template <int BD, int EPT>
-cudaError_t launch_cfg(const ChainArgs &a_in, cudaStream_t stream, int max_ctas, int *per_sm_out) {
+template <int BD, int EPT, bool SEG>
+cudaError_t launch_cfg_kernel(const ChainArgs &a_in, cudaStream_t stream, int max_ctas, int *per_sm_out) {
+    auto *const KFN = achr_chain_kernel<BD, EPT, SEG>;
     ChainArgs a = a_in;
     const size_t base = chain_smem_bytes_cfg(BD * EPT, a.d, BD);
     // The residual-form reprojection keeps z (m floats) in shared memory and
@@ -1223,15 +1227,15 @@ cudaError_t launch_cfg(const ChainArgs &a_in, cudaStream_t stream, int max_ctas,
     const size_t zbytes = ((size_t)a.m * sizeof(float) + 15) & ~(size_t)15;
     if (a.pinv32 && a.m > BD * EPT) a.pinv32 = nullptr;
     size_t smem = base + (a.pinv32 ? zbytes : 0);
-    cudaError_t e = cudaFuncSetAttribute(achr_chain_kernel<BD, EPT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaError_t e = cudaFuncSetAttribute(KFN, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)std::max(smem, base));
     if (e != cudaSuccess) return e;
     int per_sm = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, achr_chain_kernel<BD, EPT>, BD, base);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, KFN, BD, base);
     if (e != cudaSuccess) return e;
     if (a.pinv32) {
         int per_sm_z = 0;
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_z, achr_chain_kernel<BD, EPT>, BD, smem);
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_z, KFN, BD, smem);
         if (e != cudaSuccess) return e;
         if (per_sm_z < per_sm) {
             a.pinv32 = nullptr;
@@ -1248,8 +1252,16 @@ cudaError_t launch_cfg(const ChainArgs &a_in, cudaStream_t stream, int max_ctas,
     if (max_ctas > 0 && grid > max_ctas) grid = max_ctas;
     if (grid > a.P) grid = a.P;
     if (grid < 1) return cudaSuccess;
-    achr_chain_kernel<BD, EPT><<<(unsigned)grid, BD, smem, stream>>>(a);
+    KFN<<<(unsigned)grid, BD, smem, stream>>>(a);
     return cudaGetLastError();
+}
+
+// Occupancy-sized persistent launch of one configuration (segmented launches
+// take the kernel's segmented instantiation).
+template <int BD, int EPT>
+cudaError_t launch_cfg(const ChainArgs &a, cudaStream_t stream, int max_ctas, int *per_sm_out) {
+    return a.seg ? launch_cfg_kernel<BD, EPT, true>(a, stream, max_ctas, per_sm_out)
+                 : launch_cfg_kernel<BD, EPT, false>(a, stream, max_ctas, per_sm_out);
 }
 
 }  // namespace achr

@@ -70,7 +70,11 @@ achr_status ensure_reproj(achr_ctx *ctx);
 // Segmented sampling with the per-chain reprojections deferred to a batched
 // pass (achr_defer.cu): runs the launch described by `a` (a.P chains of a.T
 // steps from step 0) on `stream`.
-achr_status defer_sample(achr_ctx *ctx, const ChainArgs &a, int threads_per_chain, cudaStream_t stream);
+achr_status defer_sample(achr_ctx *ctx, const ChainArgs &a, int threads_per_chain, cudaStream_t stream,
+                         bool timed);
+// After the stream of a timed defer_sample has completed: device time of its
+// chain-kernel launches and of its batched passes, and the chains per sweep.
+achr_status defer_times(achr_ctx *ctx, double *chain_ms, double *pass_ms, double *chains_per_sweep);
 // Whether sampling with these options takes the deferred path.
 bool defer_selected(const achr_ctx *ctx);
 }  // namespace achr
@@ -105,6 +109,7 @@ struct achr_ctx {
     double warmup_residual = 0.0;         // max |S w|_inf over the warmup points (as sampled)
     double kappa_sst = 1.0;               // condition number of S S^T on its range (from the null-space set-up)
     long long last_segments = 0;          // chain-kernel launches of the last deferred-reprojection run
+    long long last_launches = 0;          // all kernels that run launched
     achr::DevBuf<double> dirs;   // hit-and-run direction pool, n x n_dirs (leading dimension ldw)
     int n_dirs = 0;              // 0: ACHR directions (warmup point minus centre)
     achr::DevBuf<double> zeros;  // np zeros: the (unused) centre accumulator of hit-and-run chains

@@ -20,21 +20,21 @@
 //     x <- x - S^T z,   z = B r,   B = (S S^T)^+,
 //
 // z for every chain as one tensor-core GEMM Z = R B^T (three BF16 split
-// products, FP32 accumulation, achr_tc_gemm.cu); each pass then forms
-// d = S^T z, adds it to the chain's correction dx and tracks r <- r - S d, all
-// in FP32 (they are of the size of the residual, not of x).  The update lies in
-// the row space of S up to FP32 rounding, so the null-space part of x moves by
-// at most ~1e-7 of the correction, and each further pass multiplies what is
-// left of the row-space part by roughly 1.5e-6 times the condition number of
-// S S^T (about 4e-3 at 2572).  A chain takes passes until max|r| falls to
-// max(residual_tol / 100, 1e-5 of the residual its check found), so the
-// corrected point is within about 1e-5 of the correction's own size of the
-// FP64 projection; models whose S S^T has a condition number above 2e4
-// reproject in the chain kernel instead.  The next launch of the chain kernel
-// subtracts dx from the point (FP64), clips it and adds it to its centre
-// accumulator before the chain's next step, the order the reference uses.  The
-// decisions (which chains reproject) are the chain kernel's own FP64 residual,
-// identical to the check it makes when it reprojects in place.
+// products, FP32 accumulation, achr_tc_gemm.cu).  The first pass applies
+// S^T z to the point in FP64 and recomputes the true residual S x in FP64, so
+// its update leaves the null-space part of x alone to FP64 rounding and what
+// is left of the residual is measured exactly (about 1e-4 of it on the
+// generator-law models).  Later passes only move the point by that remainder:
+// they form d = S^T z, add it to a correction dx and track r <- r - S d, all in
+// FP32, and the next launch subtracts dx from the point in FP64.  A chain takes
+// passes until max|r| falls to max(residual_tol / 100, 1e-7 of the residual its
+// check found), so the corrected point is within about 1e-7 of the
+// correction's own size of the FP64 projection; models whose S S^T has a
+// condition number above 2e4 reproject in the chain kernel instead.  The next
+// launch also clips the point and adds it to its centre accumulator before the
+// chain's next step, the order the reference uses.  The decisions (which
+// chains reproject) are the chain kernel's own FP64 residual, identical to the
+// check it makes when it reprojects in place.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -42,6 +42,7 @@
 #include <cstring>
 #include <new>
 #include <string>
+#include <vector>
 
 #include "achr_ctx.h"
 
@@ -65,6 +66,14 @@ struct DeferState {
     DevBuf<int> row_orig;    // m: device row order of S -> the model's row order
     DevBuf<unsigned long long> any;  // one word per launch and pass: some chain needs that pass
     int any_cap = 0;
+    // Timing of the last run (only when requested): an event before and after every
+    // chain-kernel launch, and one at the end.
+    std::vector<cudaEvent_t> ev;
+    int ev_used = 0;
+    double chains_per_sweep = 0.0;
+    ~DeferState() {
+        for (cudaEvent_t e : ev) cudaEventDestroy(e);
+    }
 };
 
 void defer_free(DeferState *d) { delete d; }
@@ -75,6 +84,10 @@ constexpr int kDeferChunk = 131072;        // chains per sweep through the segme
 constexpr double kDeferMaxKappa = 2.0e4;   // largest condition number of S S^T the passes are used for
 constexpr int kCorrThreads = 256;
 constexpr int kMaxPasses = 8;              // passes of one deferred reprojection at most
+// A chain's passes end once max|S x| <= max(residual_tol / 100, kRelTol times the residual its
+// check found): the point is then within about that fraction of the correction's size of the
+// FP64 projection (the correction is the residual's preimage).
+constexpr float kRelTol = 1e-7f;
 
 achr_status set_err(achr_status st, const std::string &msg) {
     achr_io_set_error(msg.c_str());
@@ -92,56 +105,58 @@ __global__ void to_f32_kernel(long long count, const double *__restrict__ in, fl
     if (t < count) out[t] = __double2float_rn(in[t]);
 }
 
-// One pass for every chain still flagged SEG_REPROJ (a CTA per chain at a
-// time; chain-major rows, so every load and store is coalesced):
-//     d = S^T z,  dx += d,  r <- r - S d,
-// z the chain's row of the GEMM's B (S x).  Everything here is FP32: z itself
-// carries the GEMM's error, d is at most the size of the residual's preimage,
-// and r is tracked from the chain kernel's FP64 residual by subtracting S d,
-// so FP32 rounding stays relative to the residual, not to x; the point itself
-// is touched once, in FP64, when the next launch subtracts dx.  A chain whose
-// max|r| falls to max(fine_tol, 1e-5 max|r0|) is done (flag cleared); any other
-// has r split into R for the next pass and marks that pass as needed.  After
-// the last pass a chain still above residual_tol raises ERR_DEFER_DIVERGED.  S
-// is read in the model's row order (CSC for S^T z, CSR for S d), matching B.
+// The first pass, in FP64, for every chain flagged SEG_REPROJ (a CTA per chain
+// at a time, chain-major rows): x <- x - S^T z1 and r1 = S x, both FP64, with z1
+// the GEMM's row of that chain.  This pass removes nearly all of the residual
+// (what is left is ~1e-4 of it), so its update must not leak into the null
+// space and r1 must be the true residual of the new point: both are FP64 here,
+// and the later passes, which only move the point by what is left, run in FP32.
+// r1 goes to Rf (FP32) and R (BF16 hi/lo); max|r| of the chain's check (from
+// Rf before the update) to r0; convergence as in defer_pass_kernel.
 __global__ void __launch_bounds__(kCorrThreads)
-    defer_pass_kernel(int n, int m, int kpad, int P, int pass, unsigned *__restrict__ flags,
-                      const float *__restrict__ Z, float *__restrict__ Rf, long long ldz, float *__restrict__ DX,
-                      long long ldx, float *__restrict__ r0, const int *__restrict__ cp, const int *__restrict__ ri,
-                      const float *__restrict__ cv, const int *__restrict__ rp, const int *__restrict__ ci,
-                      const float *__restrict__ rv, __nv_bfloat16 *__restrict__ Rh, __nv_bfloat16 *__restrict__ Rl,
-                      float fine_tol, float residual_tol, int last, unsigned long long *next_any,
-                      unsigned long long *counters) {
+    defer_first_pass_kernel(int n, int m, int kpad, int P, unsigned *__restrict__ flags, const float *__restrict__ Z,
+                            float *__restrict__ Rf, long long ldz, double *__restrict__ X, long long ldx,
+                            float *__restrict__ r0, const int *__restrict__ cp, const int *__restrict__ ri,
+                            const double *__restrict__ cv, const int *__restrict__ rp, const int *__restrict__ ci,
+                            const double *__restrict__ rv, __nv_bfloat16 *__restrict__ Rh,
+                            __nv_bfloat16 *__restrict__ Rl, float fine_tol, float rel_tol, float residual_tol,
+                            int last, const unsigned long long *this_gate, unsigned long long *next_any,
+                            unsigned long long *counters) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ float wmax[kCorrThreads / 32][2];
-    float *zs = reinterpret_cast<float *>(smem_raw);
-    float *ds = zs + ldz;
+    double *zd = reinterpret_cast<double *>(smem_raw);
+    double *xs = zd + ldz;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (*this_gate == 0ull) return;  // no chain's check fired (the GEMM did not run either)
+    if (blockIdx.x == 0 && tid == 0) atomicAdd(counters + CNT_GEMMS, 1ull);
     for (int p = blockIdx.x; p < P; p += gridDim.x) {
         if (!(flags[p] & SEG_REPROJ)) continue;  // uniform over the block
         const float *zp = Z + (size_t)p * (size_t)ldz;
-        for (int i = tid; i < m; i += kCorrThreads) zs[i] = zp[i];
-        __syncthreads();
-        float *dxp = DX + (size_t)p * (size_t)ldx;
-        for (int j = tid; j < n; j += kCorrThreads) {
-            float dl = 0.0f;
-            const int q1 = __ldg(cp + j + 1);
-            for (int q = __ldg(cp + j); q < q1; ++q) dl = fmaf(__ldg(cv + q), zs[__ldg(ri + q)], dl);
-            ds[j] = dl;
-            dxp[j] = pass == 0 ? dl : dxp[j] + dl;
+        float *rp_ = Rf + (size_t)p * (size_t)ldz;
+        float m0 = 0.0f;
+        for (int i = tid; i < m; i += kCorrThreads) {
+            zd[i] = (double)zp[i];
+            m0 = fmaxf(m0, fabsf(rp_[i]));
         }
         __syncthreads();
-        float *rp_ = Rf + (size_t)p * (size_t)ldz;
+        double *xp = X + (size_t)p * (size_t)ldx;
+        for (int j = tid; j < n; j += kCorrThreads) {
+            double dl = 0.0;
+            const int q1 = __ldg(cp + j + 1);
+            for (int q = __ldg(cp + j); q < q1; ++q) dl = fma(__ldg(cv + q), zd[__ldg(ri + q)], dl);
+            const double xv = xp[j] - dl;
+            xp[j] = xv;
+            xs[j] = xv;
+        }
+        __syncthreads();
         __nv_bfloat16 *rh = Rh + (size_t)p * (size_t)kpad, *rl = Rl + (size_t)p * (size_t)kpad;
-        float mx = 0.0f, m0 = 0.0f;
+        float mx = 0.0f;
         for (int i = tid; i < m; i += kCorrThreads) {
-            const float ro = rp_[i];
-            float acc = 0.0f;
+            double acc = 0.0;
             const int q1 = __ldg(rp + i + 1);
-            for (int q = __ldg(rp + i); q < q1; ++q) acc = fmaf(__ldg(rv + q), ds[__ldg(ci + q)], acc);
-            const float rn = ro - acc;
+            for (int q = __ldg(rp + i); q < q1; ++q) acc = fma(__ldg(rv + q), xs[__ldg(ci + q)], acc);
+            const float rn = __double2float_rn(acc);
             rp_[i] = rn;
-            m0 = fmaxf(m0, fabsf(ro));
             mx = fmaxf(mx, fabsf(rn));
             if (!last) {
                 const __nv_bfloat16 hi = __float2bfloat16_rn(rn);
@@ -164,9 +179,88 @@ __global__ void __launch_bounds__(kCorrThreads)
                 mx = fmaxf(mx, wmax[w][0]);
                 m0 = fmaxf(m0, wmax[w][1]);
             }
-            if (pass == 0) r0[p] = m0;  // the residual the chain's check found
-            const float target = fmaxf(fine_tol, 1e-5f * (pass == 0 ? m0 : r0[p]));
-            if (mx <= target) {
+            atomicAdd(counters + CNT_PASSES, 1ull);
+            r0[p] = m0;  // the residual the chain's check found
+            if (mx <= fmaxf(fine_tol, rel_tol * m0)) {
+                flags[p] &= ~SEG_REPROJ;  // converged
+            } else if (!last) {
+                if (*next_any == 0ull) atomicOr(next_any, 1ull);
+            } else if (mx > residual_tol) {
+                atomicOr(counters + CNT_ERROR, (unsigned long long)ERR_DEFER_DIVERGED);
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// A later pass (pass >= 1) for every chain still flagged SEG_REPROJ (a CTA
+// per chain at a time; chain-major rows, so every load and store is coalesced):
+//     d = S^T z,  dx += d,  r <- r - S d,
+// z the chain's row of the GEMM's B r.  Everything here is FP32: after the
+// first pass the residual is ~1e-4 of what the check found, d is of that size,
+// and r is tracked from the first pass's FP64 residual, so FP32 rounding stays
+// relative to what is left, not to x; the point is touched once, in FP64, when
+// the next launch subtracts dx (SEG_CORR).  A chain whose max|r| falls to
+// max(fine_tol, rel_tol max|r0|) is done (flag cleared); any other has r split
+// into R for the next pass and marks that pass as needed.  After the last pass
+// a chain still above residual_tol raises ERR_DEFER_DIVERGED.  S is read in the
+// model's row order (CSC for S^T z, CSR for S d), matching B.
+__global__ void __launch_bounds__(kCorrThreads)
+    defer_pass_kernel(int n, int m, int kpad, int P, int pass, unsigned *__restrict__ flags,
+                      const float *__restrict__ Z, float *__restrict__ Rf, long long ldz, float *__restrict__ DX,
+                      long long ldx, float *__restrict__ r0, const int *__restrict__ cp, const int *__restrict__ ri,
+                      const float *__restrict__ cv, const int *__restrict__ rp, const int *__restrict__ ci,
+                      const float *__restrict__ rv, __nv_bfloat16 *__restrict__ Rh, __nv_bfloat16 *__restrict__ Rl,
+                      float fine_tol, float rel_tol, float residual_tol, int last,
+                      const unsigned long long *this_gate, unsigned long long *next_any,
+                      unsigned long long *counters) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ float wmax[kCorrThreads / 32];
+    float *zs = reinterpret_cast<float *>(smem_raw);
+    float *ds = zs + ldz;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (*this_gate == 0ull) return;  // no chain needed this pass (its GEMM did not run either)
+    if (blockIdx.x == 0 && tid == 0) atomicAdd(counters + CNT_GEMMS, 1ull);
+    for (int p = blockIdx.x; p < P; p += gridDim.x) {
+        if (!(flags[p] & SEG_REPROJ)) continue;  // uniform over the block
+        const float *zp = Z + (size_t)p * (size_t)ldz;
+        for (int i = tid; i < m; i += kCorrThreads) zs[i] = zp[i];
+        __syncthreads();
+        float *dxp = DX + (size_t)p * (size_t)ldx;
+        for (int j = tid; j < n; j += kCorrThreads) {
+            float dl = 0.0f;
+            const int q1 = __ldg(cp + j + 1);
+            for (int q = __ldg(cp + j); q < q1; ++q) dl = fmaf(__ldg(cv + q), zs[__ldg(ri + q)], dl);
+            ds[j] = dl;
+            dxp[j] = pass == 1 ? dl : dxp[j] + dl;
+        }
+        __syncthreads();
+        float *rp_ = Rf + (size_t)p * (size_t)ldz;
+        __nv_bfloat16 *rh = Rh + (size_t)p * (size_t)kpad, *rl = Rl + (size_t)p * (size_t)kpad;
+        float mx = 0.0f;
+        for (int i = tid; i < m; i += kCorrThreads) {
+            const float ro = rp_[i];
+            float acc = 0.0f;
+            const int q1 = __ldg(rp + i + 1);
+            for (int q = __ldg(rp + i); q < q1; ++q) acc = fmaf(__ldg(rv + q), ds[__ldg(ci + q)], acc);
+            const float rn = ro - acc;
+            rp_[i] = rn;
+            mx = fmaxf(mx, fabsf(rn));
+            if (!last) {
+                const __nv_bfloat16 hi = __float2bfloat16_rn(rn);
+                rh[i] = hi;
+                rl[i] = __float2bfloat16_rn(rn - __bfloat162float(hi));
+            }
+        }
+#pragma unroll
+        for (int o = 16; o; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        if (lane == 0) wmax[warp] = mx;
+        __syncthreads();
+        if (tid == 0) {
+            for (int w = 1; w < kCorrThreads / 32; ++w) mx = fmaxf(mx, wmax[w]);
+            atomicAdd(counters + CNT_PASSES, 1ull);
+            if (pass == 1) flags[p] |= SEG_CORR;  // dx now holds a correction for the next launch
+            if (mx <= fmaxf(fine_tol, rel_tol * r0[p])) {
                 flags[p] &= ~SEG_REPROJ;  // converged
             } else if (!last) {
                 if (*next_any == 0ull) atomicOr(next_any, 1ull);
@@ -238,7 +332,7 @@ bool defer_selected(const achr_ctx *ctx) {
     return ctx->warmup_residual > o.residual_tol / 8.0 && (double)ctx->n * (double)ctx->d >= 2.5e5;
 }
 
-achr_status defer_sample(achr_ctx *ctx, const ChainArgs &a_in, int threads_per_chain, cudaStream_t s) {
+achr_status defer_sample(achr_ctx *ctx, const ChainArgs &a_in, int threads_per_chain, cudaStream_t s, bool timed) {
     achr_status st = ensure_reproj(ctx);
     if (st != ACHR_OK) return st;
     // Steps [S0, E) of every chain (S0 > 0: chains resumed from a_in.x_in / A_in).
@@ -251,21 +345,38 @@ achr_status defer_sample(achr_ctx *ctx, const ChainArgs &a_in, int threads_per_c
     if (st != ACHR_OK) return st;
     DeferState &D = *ctx->defer;
     const ReprojState &R = *ctx->reproj;
+    D.ev_used = 0;
+    D.chains_per_sweep = (double)P / (double)((P + cap - 1) / cap);
+    auto mark = [&]() -> cudaError_t {  // record the next timing event on the stream
+        if (!timed) return cudaSuccess;
+        if (D.ev_used == (int)D.ev.size()) {
+            cudaEvent_t e = nullptr;
+            cudaError_t ce = cudaEventCreate(&e);
+            if (ce != cudaSuccess) return ce;
+            D.ev.push_back(e);
+        }
+        return cudaEventRecord(D.ev[(size_t)D.ev_used++], s);
+    };
     const int passes = ctx->opt.reprojection_passes > 0 ? ctx->opt.reprojection_passes : kMaxPasses;
-    // A chain's passes end once max|S x| <= max(residual_tol / 100, 1e-5 of the residual its check
-    // found): the point is then within about that over the smallest singular value of S of the
-    // FP64 projection, i.e. within 1e-5 of the correction's own size.
     const double fine_tol = ctx->opt.residual_tol * 0.01;
 
     int dev = 0, sms = 0, per_sm = 0;
     DEFER_TRY(cudaGetDevice(&dev));
     DEFER_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     const size_t corr_smem = sizeof(float) * ((size_t)D.ldz + (size_t)D.ld);
+    const size_t first_smem = sizeof(double) * ((size_t)D.ldz + (size_t)D.ld);
+    int per_sm1 = 0;
     DEFER_TRY(cudaFuncSetAttribute(defer_pass_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)corr_smem));
+    DEFER_TRY(cudaFuncSetAttribute(defer_first_pass_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)first_smem));
     DEFER_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, defer_pass_kernel, kCorrThreads, corr_smem));
-    if (per_sm < 1) return set_err(ACHR_ERR_UNSUPPORTED, "model too large for the batched reprojection's update");
+    DEFER_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm1, defer_first_pass_kernel, kCorrThreads,
+                                                            first_smem));
+    if (per_sm < 1 || per_sm1 < 1)
+        return set_err(ACHR_ERR_UNSUPPORTED, "model too large for the batched reprojection's update");
 
     ctx->last_segments = 0;
+    ctx->last_launches = 0;
     for (int c0 = 0; c0 < P; c0 += cap) {
         const int pc = std::min(cap, P - c0);
         DEFER_TRY(cudaMemsetAsync(D.flags.p, 0, sizeof(unsigned) * (size_t)pc, s));
@@ -291,6 +402,7 @@ achr_status defer_sample(achr_ctx *ctx, const ChainArgs &a_in, int threads_per_c
         a.ld_r = D.ldz;
         a.seg_dx = D.dx.p;
         const int corr_grid = (int)std::min<long long>((long long)sms * per_sm, pc);
+        const int first_grid = (int)std::min<long long>((long long)sms * per_sm1, pc);
         int s0 = S0, seg = 0;
         for (;;) {
             // The launch runs to the first check step at or after s0 (the reference
@@ -302,8 +414,11 @@ achr_status defer_sample(achr_ctx *ctx, const ChainArgs &a_in, int threads_per_c
             a.seg_final = ends_on_check ? 0 : 1;
             unsigned long long *gate = D.any.p + (size_t)seg * (kMaxPasses + 1);
             a.seg_any = gate;  // pass 0 is needed when some chain's check fired
+            DEFER_TRY(mark());
             DEFER_TRY(launch_chains(a, threads_per_chain, s));
+            DEFER_TRY(mark());
             ++ctx->last_segments;
+            ++ctx->last_launches;
             if (!ends_on_check) break;
             for (int pass = 0; pass < passes; ++pass) {
                 TcGemm g{pc, R.m, R.kpad, 3, D.Rh.p, D.Rl.p, (long long)R.kpad, R.Bh.p, R.Bl.p, (long long)R.kpad,
@@ -312,12 +427,21 @@ achr_status defer_sample(achr_ctx *ctx, const ChainArgs &a_in, int threads_per_c
                 g.gate_max = 0;
                 if (const char *why = tc_gemm_check(g)) return set_err(ACHR_ERR_INVALID, why);
                 DEFER_TRY(launch_tc_gemm(g, a_in.counters + CNT_ERROR, s));
-                defer_pass_kernel<<<(unsigned)corr_grid, kCorrThreads, corr_smem, s>>>(
-                    ctx->n, ctx->m, R.kpad, pc, pass, D.flags.p, D.Z.p, D.r.p, D.ldz, D.dx.p, D.ld, D.r0.p, R.cp.p,
-                    R.ri.p, D.cv32.p, R.rp.p, R.ci.p, D.rv32.p, reinterpret_cast<__nv_bfloat16 *>(D.Rh.p),
-                    reinterpret_cast<__nv_bfloat16 *>(D.Rl.p), (float)fine_tol, (float)ctx->opt.residual_tol,
-                    pass + 1 == passes ? 1 : 0, gate + pass + 1, a_in.counters);
+                if (pass == 0)
+                    defer_first_pass_kernel<<<(unsigned)first_grid, kCorrThreads, first_smem, s>>>(
+                        ctx->n, ctx->m, R.kpad, pc, D.flags.p, D.Z.p, D.r.p, D.ldz, D.x.p, D.ld, D.r0.p, R.cp.p,
+                        R.ri.p, R.cv.p, R.rp.p, R.ci.p, R.rv.p, reinterpret_cast<__nv_bfloat16 *>(D.Rh.p),
+                        reinterpret_cast<__nv_bfloat16 *>(D.Rl.p), (float)fine_tol, kRelTol,
+                        (float)ctx->opt.residual_tol, passes == 1 ? 1 : 0, gate, gate + 1, a_in.counters);
+                else
+                    defer_pass_kernel<<<(unsigned)corr_grid, kCorrThreads, corr_smem, s>>>(
+                        ctx->n, ctx->m, R.kpad, pc, pass, D.flags.p, D.Z.p, D.r.p, D.ldz, D.dx.p, D.ld, D.r0.p,
+                        R.cp.p, R.ri.p, D.cv32.p, R.rp.p, R.ci.p, D.rv32.p,
+                        reinterpret_cast<__nv_bfloat16 *>(D.Rh.p), reinterpret_cast<__nv_bfloat16 *>(D.Rl.p),
+                        (float)fine_tol, kRelTol, (float)ctx->opt.residual_tol, pass + 1 == passes ? 1 : 0,
+                        gate + pass, gate + pass + 1, a_in.counters);
                 DEFER_TRY(cudaGetLastError());
+                ctx->last_launches += 2;
             }
             ++seg;
             s0 = c + 1;
@@ -326,12 +450,34 @@ achr_status defer_sample(achr_ctx *ctx, const ChainArgs &a_in, int threads_per_c
                 a.T = 0;
                 a.seg_final = 1;
                 a.seg_any = D.any.p + (size_t)seg * (kMaxPasses + 1);
+                DEFER_TRY(mark());
                 DEFER_TRY(launch_chains(a, threads_per_chain, s));
+                DEFER_TRY(mark());
                 ++ctx->last_segments;
+                ++ctx->last_launches;
                 break;
             }
         }
     }
+    DEFER_TRY(mark());
+    return ACHR_OK;
+}
+
+achr_status defer_times(achr_ctx *ctx, double *chain_ms, double *pass_ms, double *chains_per_sweep) {
+    DeferState *D = ctx->defer;
+    double c = 0.0, q = 0.0;
+    if (D) {
+        // events: (before, after) of every chain-kernel launch, then one at the end
+        for (int k = 0; k + 1 < D->ev_used; ++k) {
+            float ms = 0.0f;
+            DEFER_TRY(cudaEventElapsedTime(&ms, D->ev[(size_t)k], D->ev[(size_t)k + 1]));
+            if (k % 2 == 0) c += ms;
+            else q += ms;
+        }
+    }
+    *chain_ms = c;
+    *pass_ms = q;
+    *chains_per_sweep = D ? D->chains_per_sweep : 0.0;
     return ACHR_OK;
 }
 

@@ -19,6 +19,8 @@ enum CounterSlot {
     CNT_MAXRES_BITS = 7,   // max ||S v||_inf of emitted points, as the bits of a non-negative double
     CNT_MAXVIOL_BITS = 8,  // max bound violation of emitted points, same encoding
     CNT_ERROR = 9,         // bit flags, ERR_*
+    CNT_PASSES = 10,       // deferred reprojection: chain-passes (one chain through one batched pass)
+    CNT_GEMMS = 11,        // deferred reprojection: tensor-core GEMMs that ran (not skipped by their gate)
     CNT_SLOTS = 16
 };
 

@@ -54,6 +54,7 @@ def parse_args():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-ess", action="store_true", help="skip the bounded min-ESS/s and R-hat leg")
+    ap.add_argument("--no-exact-leg", action="store_true", help="skip the short exact-warmup comparison")
     ap.add_argument("--ess", type=int, nargs=4, metavar=("CHAINS", "BURNIN", "SEGMENTS", "STEPS"),
                     help="min-ESS/s and max R-hat from trace snapshots: CHAINS chains, BURNIN steps, then SEGMENTS "
                          "snapshots STEPS steps apart")
@@ -78,7 +79,7 @@ def parse_args():
     ap.add_argument("--large-chains", type=int, default=262_144, help="chains of the large workload")
     ap.add_argument("--large-steps", type=int, default=200, help="timed steps of the large workload")
     ap.add_argument("--threads-per-chain", type=int, default=0, help="chain-kernel block size (0: by model size)")
-    ap.add_argument("--warmup-form", choices=["percent_f", "exact"], default="exact",
+    ap.add_argument("--warmup-form", choices=["percent_f", "exact"], default="percent_f",
                     help="warmup points as the reference's %%f CSV holds them, or exact FP64 chord points")
     ap.add_argument("--chains", type=int, default=0, help="override the workload's chain count (0: its own)")
     ap.add_argument("--bracket-pass", type=int, choices=[0, 1], default=0,
@@ -373,9 +374,10 @@ def run_gpu(args):
     evs = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
     torch.cuda.synchronize()
     evs[0].record(stream)
+    timed = []  # per step: the library's own split of its device time (chain kernel / batched reprojection)
     for k in range(args.steps):
-        smp.sample_device(P, T, out.data_ptr(), P, stream.cuda_stream, seed=args.seed + 1000 + k,
-                          chain_offset=chain_base)
+        timed.append(smp.sample_device(P, T, out.data_ptr(), P, stream.cuda_stream, seed=args.seed + 1000 + k,
+                                       chain_offset=chain_base, with_stats=True))
         evs[k + 1].record(stream)
     torch.cuda.synchronize()
     clk = clocks.stop()
@@ -387,13 +389,30 @@ def run_gpu(args):
     chain_steps = P * T
     value = world * chain_steps / (ms * 1e-3)
 
+    # Roofline of the dominant kernel, the chain kernel: its algorithmic bytes over its own device
+    # time (CUDA events around its launches on the launch stream, inside the library).
     peak, peak_kind = load_peaks()
     alg_bytes = synth.ideal_bytes_per_chain_step(n) * chain_steps
-    achieved = alg_bytes / (ms * 1e-3) / 1e9
+    chain_ms = sum(s["chain_ms"] for s in timed) / len(timed)
+    launches = max(1, int(round(sum(max(1, s["segments"]) for s in timed) / len(timed))))
+    achieved = alg_bytes / (chain_ms * 1e-3) / 1e9
     tpcs = profile_traffic_per_chain_step(args.workload)
-    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": (tpcs * chain_steps) if tpcs is not None else None,
-                "peak_source": f"{peak_kind} hbm_gbs", "algorithmic_bytes_per_launch": alg_bytes}
+    roofline = {"bound": "hbm", "kernel": "achr_chain_kernel", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": (tpcs * chain_steps) if tpcs is not None else None,
+                "peak_source": f"{peak_kind} hbm_gbs (burst copy)", "algorithmic_bytes_per_step": alg_bytes,
+                "kernel_ms_per_step": chain_ms, "kernel_launches_per_step": launches,
+                "whole_step_frac": alg_bytes / (ms * 1e-3) / 1e9 / peak}
+    reproj = None
+    rms = sum(s["reprojection_ms"] for s in timed) / len(timed)
+    if rms > 0:
+        tpk, tpk_kind = load_tensor_peak()
+        rfl = sum(s["reprojection_flops"] for s in timed) / len(timed)
+        reproj = {"form": "deferred batched (three BF16 split products on the tensor cores, FP32 passes)",
+                  "ms_per_step": rms, "share_of_step": rms / ms,
+                  "chain_passes_per_reprojection": timed[-1]["reprojection_passes"] / max(1, timed[-1]["reprojections"]),
+                  "gemms_per_step": timed[-1]["reprojection_gemms"], "gemm_tflop_per_step": rfl / 1e12,
+                  "tensor_tflops_over_pass_time": rfl / (rms * 1e-3) / 1e12, "tensor_peak_tflops": tpk,
+                  "tensor_peak_source": tpk_kind}
 
     # End to end through the public API with host buffers: set-up from pinned host
     # model + warmup (H2D, null space, centre), sampling, D2H of every point.
@@ -427,6 +446,20 @@ def run_gpu(args):
     if rank == 0 and world == 1 and not args.no_ess:
         ess = ess_leg(pkg, synth, args, (spec, model, warm))
 
+    # The same workload on exact (unrounded) warmup points, where the reference's residual check
+    # never fires: the sampling step alone, for comparison with the %f figure above.
+    exact = None
+    if rank == 0 and world == 1 and args.warmup_form == "percent_f" and not args.no_exact_leg:
+        _, model_x, _, warm_x, _, _ = build_inputs(args.workload, pkg, synth, warmup_form="exact")
+        with pkg.Sampler(model_x, warm_x, **sampler_options(args)) as sx:
+            sx.sample_device(P, T, out.data_ptr(), P, stream.cuda_stream, seed=args.seed)
+            xs = [sx.sample_device(P, T, out.data_ptr(), P, stream.cuda_stream, seed=args.seed + 7000 + k,
+                                   with_stats=True) for k in range(3)]
+        xms = sum(s["kernel_ms"] for s in xs) / len(xs)
+        exact = {"value": chain_steps / (xms * 1e-3), "unit": METRIC, "steps": len(xs), "ms_per_step": xms,
+                 "roofline_frac": alg_bytes / (xms * 1e-3) / 1e9 / peak,
+                 "reprojections": xs[-1]["reprojections"], "segments": xs[-1]["segments"]}
+
     line = {
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
@@ -435,16 +468,22 @@ def run_gpu(args):
                                f"{P} chains x {T} steps per GPU, mode=reference, warmups {args.warmup_form}",
                    "global_batch": world * P, "seq_len": T, "parallelism": f"chains sharded over {world} GPU(s)",
                    "l2": "inputs exceed L2 (warmup matrix 224 MB > 129 MB); no flush",
+                   "warmups": ("the reference's input form: chord points written with %f and read back, as "
+                               "VFWarmup/createWarmupPtsGLPK.c writes them, so the 10-step checks reproject"
+                               if args.warmup_form == "percent_f" else "exact FP64 chord points"),
                    "options": sampler_options(args)},
-        "gpu_launches": args.steps,
+        "gpu_launches": int(sum(s["kernel_launches"] for s in timed)),
         "roofline": roofline,
         "cpu_baseline": cpu,
         "e2e": e2e,
         "clocks": clk,
         "ess": ess,
+        "reprojection": reproj,
+        "exact_warmups": exact,
         "sampler": {"null_dim": smp.null_dim, "setup_s": setup_s,
                     **({k: stats[k] for k in ("accepted", "rejected", "checks", "reprojections", "stuck_chains",
-                                              "exact_evals", "max_residual", "max_bound_violation", "segments")}
+                                              "exact_evals", "max_residual", "max_bound_violation", "segments",
+                                              "reprojection_passes", "reprojection_gemms")}
                        if stats else {})},
     }
     if rank == 0:

@@ -90,11 +90,12 @@ typedef struct {
                                     and the chains whose residual exceeds residual_tol are reprojected
                                     together, x <- x - S^T (S S^T)^+ S x with S x and the update in FP64
                                     and the dense product on the tensor cores (three BF16 split
-                                    products), repeated per chain until max|S x| <= residual_tol / 100
-                                    (each pass multiplies the remaining error by about 1.5e-6 times the
-                                    condition number of S S^T); then the clip and the centre update of
-                                    that step, as the reference orders them; needs n_mets <= the chain
-                                    kernel's padded length and that condition number <= 2e4 (achr_sample,
+                                    products); the first pass updates the point in FP64, later ones
+                                    (FP32, on what is left) run per chain until max|S x| <=
+                                    max(residual_tol / 100, 1e-7 of the residual the check found); then
+                                    the clip and the centre update of that step, as the reference orders
+                                    them; needs n_mets <= the chain kernel's padded length and a condition
+                                    number of S S^T <= 2e4 (achr_sample,
                                     achr_sample_device and achr_sample_resume; batched launches
                                     reproject in the chain kernel, and so does choice 0 with a
                                     hit-and-run pool) */
@@ -130,6 +131,14 @@ typedef struct {
     double kernel_ms;         /* device time of the sampling launch(es) */
     int64_t segments;         /* chain-kernel launches of deferred-reprojection sampling (reproject_form 3,
                                  or 0 choosing it); 0 when reprojections ran inside the chain kernel */
+    int64_t reprojection_passes; /* deferred: passes summed over the reprojected chains */
+    int64_t reprojection_gemms;  /* deferred: tensor-core GEMMs that ran (each over all chains of a sweep) */
+    double chain_ms;          /* device time of the chain-kernel launches alone (= kernel_ms when the
+                                 reprojections ran inside the chain kernel) */
+    double reprojection_ms;   /* deferred: device time of the batched passes (GEMMs and updates) */
+    double reprojection_flops;/* deferred: FLOPs of the GEMMs that ran (three BF16 split products) */
+    int64_t kernel_launches;  /* kernels the call launched (chain kernel, and when deferred the GEMMs and
+                                 pass kernels, including those a device-side gate then skipped) */
 } achr_stats;
 
 typedef struct achr_ctx achr_ctx;
@@ -281,6 +290,25 @@ achr_status achr_precond_train(int32_t d, int32_t r, int32_t n_samples, const fl
  * to rounding), installed with achr_set_directions. */
 achr_status achr_precond_pool(achr_ctx *ctx, int32_t r, const float *d_s, const float *d_U, int32_t n_dirs,
                               uint64_t seed);
+
+/* Pilot run of the installed direction pool and the fallback to plain ACHR.
+ * `chains` chains start at random warmup points (Philox keyed by seed), run
+ * `burnin` steps along the pool, then `draws` draws `gap` steps apart; the
+ * split-R-hat of every moving flux (Gelman et al., BDA3 11.4: halves of every
+ * chain, sqrt(((n-1)/n W + B/n) / W)) is computed on the GPU.  When its maximum
+ * is at or above rhat_limit (1.01 in the usual practice) the pool is removed and
+ * the context returns to the reference's direction rule (ACHRCuda.cu:260-264),
+ * so a preconditioner that does not mix never replaces plain ACHR.  The chains
+ * use ids 0 .. chains-1 of seed. */
+typedef struct {
+    double rhat_max;          /* largest split-R-hat over the moving fluxes */
+    int32_t fluxes;           /* fluxes that moved in the pilot (the others are left out) */
+    int32_t kept;             /* 1: the pool stays installed; 0: removed (plain ACHR) */
+    double sampling_ms;       /* device time of the pilot's sampling launches */
+} achr_direction_check;
+
+achr_status achr_check_directions(achr_ctx *ctx, int32_t chains, int32_t burnin, int32_t draws, int32_t gap,
+                                  uint64_t seed, double rhat_limit, achr_direction_check *out);
 
 /* ---- Batched reprojection on the tensor cores and periodic-reprojection
  * sampling.  The reference reprojects one chain at a time when its residual

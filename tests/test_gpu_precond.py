@@ -212,3 +212,27 @@ def test_learned_pool_directions_lie_in_null_space(pkg, small_model, golden):
     assert st["accepted"] == 128 * 40 and st["stuck_chains"] == 0
     assert np.abs(S @ pts).max() <= 1e-8
     assert np.all(pts >= small_model.lb[:, None] - 1e-9) and np.all(pts <= small_model.ub[:, None] + 1e-9)
+
+
+def test_check_directions_falls_back_to_plain_achr(pkg, small_model, golden):
+    """A pool that cannot mix (one direction: every chain stays on its own line through its
+    starting warmup point) fails the split-R-hat check and is removed; a pool spanning the
+    polytope's affine hull passes and stays."""
+    with pkg.Sampler(small_model, golden["warmup"]) as s:
+        s.set_null_space(golden["N"])
+        Bas = s.precond_basis()
+        s.set_directions(Bas[:, :1])
+        chk = s.check_directions(chains=128, burnin=2000, draws=40, gap=50, seed=3)
+        assert chk["kept"] == 0 and chk["rhat_max"] >= 1.01 and chk["fluxes"] > 0
+        assert s.directions().shape[1] == 0  # back to ACHR
+        rng = np.random.default_rng(4)
+        s.set_directions(Bas @ rng.standard_normal((Bas.shape[1], 8192)))
+        chk = s.check_directions(chains=256, burnin=20000, draws=100, gap=200, seed=3, rhat_limit=1.05)
+        assert chk["kept"] == 1 and chk["rhat_max"] < 1.05, chk
+        assert s.directions().shape[1] == 8192
+
+
+def test_check_directions_needs_a_pool(pkg, sampler):
+    with pytest.raises(pkg.AchrError) as e:
+        sampler.check_directions()
+    assert e.value.status == 1
