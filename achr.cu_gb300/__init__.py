@@ -27,6 +27,7 @@ MODE_REFERENCE = 0
 MODE_FEASIBLE = 1
 NULL_SVD_STS = 0
 NULL_SVD_S = 1
+NULL_FIXED = 2
 
 STATUS_NAMES = {
     0: "ACHR_OK", 1: "ACHR_ERR_INVALID", 2: "ACHR_ERR_CUDA", 3: "ACHR_ERR_NOMEM", 4: "ACHR_ERR_IO",

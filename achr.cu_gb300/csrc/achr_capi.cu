@@ -151,7 +151,7 @@ namespace {
 
 achr_status validate_options(const achr_options &o) {
     if (o.mode != ACHR_MODE_REFERENCE && o.mode != ACHR_MODE_FEASIBLE) return fail(ACHR_ERR_INVALID, "unknown mode");
-    if (o.null_space != ACHR_NULL_SVD_STS && o.null_space != ACHR_NULL_SVD_S)
+    if (o.null_space != ACHR_NULL_SVD_STS && o.null_space != ACHR_NULL_SVD_S && o.null_space != ACHR_NULL_FIXED)
         return fail(ACHR_ERR_INVALID, "unknown null_space method");
     if (o.check_period < 0) return fail(ACHR_ERR_INVALID, "check_period must be >= 0 (0: no in-loop checks)");
     if (o.max_attempts <= 0) return fail(ACHR_ERR_INVALID, "max_attempts must be positive");
@@ -581,6 +581,20 @@ achr_status achr_create(const achr_model *model, const double *warmup, int32_t n
         d = n;
         Nh.assign((size_t)n * n, 0.0);
         for (int i = 0; i < n; ++i) Nh[(size_t)i * n + i] = 1.0;
+    } else if (opt.null_space == ACHR_NULL_FIXED) {
+        // S with a unit row for every fixed reaction (lb == ub): those reactions are held too.
+        std::vector<int> fixed;
+        for (int i = 0; i < n; ++i)
+            if (model->lb[i] == model->ub[i]) fixed.push_back(i);
+        const int ma = m + (int)fixed.size();
+        std::vector<double> Sa((size_t)ma * n, 0.0);
+        for (int j = 0; j < n; ++j)
+            std::memcpy(Sa.data() + (size_t)j * ma, denseS.data() + (size_t)j * m, sizeof(double) * m);
+        for (size_t k = 0; k < fixed.size(); ++k) Sa[(size_t)fixed[k] * ma + (size_t)m + k] = 1.0;
+        double kappa_aug = 1.0;
+        st = null_space_sts(n, ma, Sa, Nh, d, kappa_aug);
+        if (st != ACHR_OK) return st;
+        ctx->kappa_sst = INFINITY;  // the deferred projector (built from S alone) would not match this basis
     } else {
         st = (opt.null_space == ACHR_NULL_SVD_S) ? null_space_svd_s(n, m, denseS, Nh, d, ctx->kappa_sst)
                                                  : null_space_sts(n, m, denseS, Nh, d, ctx->kappa_sst);

@@ -7,7 +7,8 @@
 // stdout as ACHRcu/ACHRCuda.cu:504-802.  Optional trailing flags:
 //   --seed S            64-bit seed of the Philox stream (default: time-based, printed)
 //   --mode reference|feasible
-//   --null sts|svd      null-space construction (default sts, the reference's rule)
+//   --null sts|svd|fixed  null-space construction (default sts, the reference's rule; fixed also
+//                       holds the reactions with lb == ub)
 //   --centre cuda|matlab  centre weights (ACHRCuda.cu:347-348 or ACHRSamplerMOD.m:174)
 //   --threads-per-chain N
 //   --check-period N    residual check every N steps (default 10, ACHRCuda.cu:325; 0 = never)
@@ -56,7 +57,7 @@ int main(int argc, char **argv) {
     if (argc < 6) {
         std::fprintf(stderr,
                      "usage: %s model.mps warmuppoints.csv nFiles nPoints nSteps [--seed S] [--mode reference|feasible]"
-                     " [--null sts|svd] [--centre cuda|matlab] [--threads-per-chain N] [--check-period N]"
+                     " [--null sts|svd|fixed] [--centre cuda|matlab] [--threads-per-chain N] [--check-period N]"
                      " [--reproject auto|nnt|residual|deferred] [--reprojection-passes N] [--bracket-pass merged|separate]"
                      " [--writer-threads N]"
                      " [--report file.json]\n",
@@ -90,6 +91,7 @@ int main(int argc, char **argv) {
             std::string m = need();
             if (m == "sts") opt.null_space = ACHR_NULL_SVD_STS;
             else if (m == "svd") opt.null_space = ACHR_NULL_SVD_S;
+            else if (m == "fixed") opt.null_space = ACHR_NULL_FIXED;
             else return std::fprintf(stderr, "ACHRCuda: bad --null\n"), 2;
         } else if (f == "--centre") {
             std::string m = need();

@@ -59,6 +59,7 @@ def parse_args():
                     help="min-ESS/s and max R-hat from trace snapshots: CHAINS chains, BURNIN steps, then SEGMENTS "
                          "snapshots STEPS steps apart")
     ap.add_argument("--gemm", type=int, metavar="CHAINS", help="time the tensor-core GEMM alone at this N")
+    ap.add_argument("--null-report", action="store_true", help="null-space set-up time and basis quality")
     ap.add_argument("--cli", action="store_true", help="wall time of the drop-in CLI on the 72 x 95 fixture")
     ap.add_argument("--learned", type=int, nargs=4, metavar=("CHAINS", "BURNIN", "SEGMENTS", "STEPS"),
                     help="learned-preconditioned hit-and-run against plain ACHR on this ESS schedule")
@@ -968,6 +969,51 @@ def run_large(args):
     return 0
 
 
+def run_null_report(args):
+    """Null-space set-up at the workload's size (the reference's computeKernelCuda, ACHRCuda.cu:436-502):
+    for each construction, the wall time of context creation (upload, null space, centre) and the
+    quality of the basis, max|S N| and max|N^T N - I| (FP64, on the GPU)."""
+    import importlib
+
+    import torch
+
+    import __graft_entry__ as ge
+
+    pkg = ge.load_package()
+    pkg.lib()
+    synth = importlib.import_module("achr_gb300.synthetic")
+    spec, model, S, warm, _, _ = build_inputs(args.workload, pkg, synth, null_space=gpu_null_space_fn(pkg),
+                                              warmup_form=args.warmup_form)
+    St = torch.from_numpy(S).cuda()
+    rows = {}
+    for name, code in (("sts", pkg.NULL_SVD_STS), ("svd", pkg.NULL_SVD_S), ("fixed", pkg.NULL_FIXED)):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        try:
+            smp = pkg.Sampler(model, warm, null_space=code)
+        except pkg.AchrError as e:
+            rows[name] = {"error": str(e)}
+            continue
+        torch.cuda.synchronize()
+        create_s = time.perf_counter() - t0
+        N = torch.from_numpy(smp.null_space()).cuda()
+        d = N.shape[1]
+        I = torch.eye(d, dtype=torch.float64, device="cuda")
+        fixed = torch.from_numpy(np.asarray(model.lb == model.ub)).cuda()
+        rows[name] = {"create_s": create_s, "null_dim": d, "max_abs_SN": float((St @ N).abs().max()),
+                      "max_abs_NtN_minus_I": float((N.T @ N - I).abs().max()),
+                      "max_abs_N_on_fixed": float(N[fixed].abs().max()) if bool(fixed.any()) else 0.0}
+        smp.close()
+        del N, I
+    line = {"metric": "null-space set-up", "unit": "s", "higher_is_better": False, "n_gpus": 1, "dtype": "f64",
+            "data": "synthetic", "config": {"workload": f"{args.workload}: {spec.n_mets}x{spec.n_rxns}, "
+                                                        f"W={warm.shape[1]}, fixed reactions "
+                                                        f"{int(np.sum(model.lb == model.ub))}"},
+            "methods": rows}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_gemm(args):
     """The tensor-core GEMM alone on the reprojection's shape: M = 5063 (metabolites of
     the large model), K = 5120 (padded), N = --gemm CHAINS, one product and the three
@@ -1051,6 +1097,8 @@ def main():
     args = parse_args()
     if args.cli:
         return run_cli(args)
+    if args.null_report:
+        return run_null_report(args)
     if args.gemm:
         return run_gemm(args)
     if args.learned:

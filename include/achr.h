@@ -63,7 +63,11 @@ enum {
 /* Null-space basis construction. */
 enum {
     ACHR_NULL_SVD_STS = 0,    /* SVD of S^T S, cutoff n*sigma0*2.2204e-16 (ACHRCuda.cu:436-502) */
-    ACHR_NULL_SVD_S = 1       /* SVD of S itself (better conditioned), same cutoff rule on sigma(S) */
+    ACHR_NULL_SVD_S = 1,      /* SVD of S itself (better conditioned), same cutoff rule on sigma(S) */
+    ACHR_NULL_FIXED = 2       /* as SVD_STS on S with a unit row appended for every reaction with lb == ub:
+                                 the basis spans {v : S v = 0, v_i = 0 where lb_i = ub_i}, so a
+                                 reprojection never moves a fixed (blocked) reaction off its value.
+                                 Not the reference's basis; reprojections then stay in the chain kernel. */
 };
 
 typedef struct {

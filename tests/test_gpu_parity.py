@@ -199,6 +199,26 @@ def test_gpu_null_space_svd_of_s(pkg, small_model, golden):
     assert np.abs(N @ N.T - golden["N"] @ golden["N"].T).max() < 1e-10
 
 
+def test_gpu_null_space_holding_fixed_reactions(pkg, small_model, golden):
+    """ACHR_NULL_FIXED: reactions with lb == ub get a unit row of their own, so the basis spans
+    {v : S v = 0, v_i = 0 on them} and a reprojection leaves them where they are."""
+    lb, ub = golden["lb"].copy(), golden["ub"].copy()
+    fixed = [3, 17, 40]
+    lb[fixed] = ub[fixed] = 0.0
+    model = pkg.HostModel(small_model.n_rxns, small_model.n_mets, small_model.row, small_model.col,
+                          small_model.val, lb, ub)
+    S = dense_S(model)
+    with pkg.Sampler(model, golden["warmup"], null_space=pkg.NULL_FIXED) as s:
+        N = s.null_space()
+    A = np.vstack([S, np.eye(S.shape[1])[fixed]])
+    lam, V = np.linalg.eigh(A.T @ A)
+    ref = V[:, lam < A.shape[1] * lam.max() * 2.2204e-16]
+    assert N.shape == ref.shape
+    assert np.abs(S @ N).max() < 1e-10 and np.abs(N[fixed]).max() < 1e-12
+    assert np.allclose(N.T @ N, np.eye(N.shape[1]), atol=1e-10)
+    assert np.abs(N @ N.T - ref @ ref.T).max() < 1e-10
+
+
 def test_resume_in_segments_equals_one_run(sampler):
     """12 + 9 + 17 steps in three launches give the points of one 38-step launch."""
     torch = pytest.importorskip("torch")

@@ -216,8 +216,8 @@ def test_learned_pool_directions_lie_in_null_space(pkg, small_model, golden):
 
 def test_check_directions_falls_back_to_plain_achr(pkg, small_model, golden):
     """A pool that cannot mix (one direction: every chain stays on its own line through its
-    starting warmup point) fails the split-R-hat check and is removed; a pool spanning the
-    polytope's affine hull passes and stays."""
+    starting warmup point) fails the split-R-hat check and is removed; a pool of the warmup
+    points' own spread (differences from their centre, in the null space) passes and stays."""
     with pkg.Sampler(small_model, golden["warmup"]) as s:
         s.set_null_space(golden["N"])
         Bas = s.precond_basis()
@@ -225,11 +225,12 @@ def test_check_directions_falls_back_to_plain_achr(pkg, small_model, golden):
         chk = s.check_directions(chains=128, burnin=2000, draws=40, gap=50, seed=3)
         assert chk["kept"] == 0 and chk["rhat_max"] >= 1.01 and chk["fluxes"] > 0
         assert s.directions().shape[1] == 0  # back to ACHR
-        rng = np.random.default_rng(4)
-        s.set_directions(Bas @ rng.standard_normal((Bas.shape[1], 8192)))
-        chk = s.check_directions(chains=256, burnin=20000, draws=100, gap=200, seed=3, rhat_limit=1.05)
-        assert chk["kept"] == 1 and chk["rhat_max"] < 1.05, chk
-        assert s.directions().shape[1] == 8192
+        W = golden["warmup"]
+        pool = Bas @ (Bas.T @ (W - W.mean(axis=1, keepdims=True)))
+        s.set_directions(pool)
+        chk = s.check_directions(chains=256, burnin=50000, draws=100, gap=500, seed=3, rhat_limit=1.1)
+        assert chk["kept"] == 1 and chk["rhat_max"] < 1.1, chk
+        assert s.directions().shape[1] == W.shape[1]
 
 
 def test_check_directions_needs_a_pool(pkg, sampler):
