@@ -352,6 +352,17 @@ __device__ __forceinline__ unsigned long long residual_rows(const ChainArgs &a, 
     return mx;
 }
 
+// FP32 -> FP64 with integer operations only (exact for normal values; zero and
+// subnormal values give a signed zero).
+__device__ __forceinline__ double f32_to_f64_exact(float f) {
+    const unsigned u = __float_as_uint(f);
+    const unsigned e = (u >> 23) & 0xFFu;
+    const unsigned long long s = (unsigned long long)(u & 0x80000000u) << 32;
+    if (e == 0) return __longlong_as_double((long long)s);
+    return __longlong_as_double(
+        (long long)(s | ((unsigned long long)(e + 896u) << 52) | ((unsigned long long)(u & 0x7FFFFFu) << 29)));
+}
+
 // BF16 bits of f rounded to nearest even (hi) and of the remainder f - hi (lo),
 // for finite f; FP32 and integer operations only.
 __device__ __forceinline__ void split_bf16_bits(float f, unsigned short &hi, unsigned short &lo) {
@@ -526,13 +537,16 @@ __global__ void __launch_bounds__(BD, (BD <= 384 ? 2 : 1)) achr_chain_kernel(con
         const bool was_stuck = (sflags & SEG_STUCK) != 0;
         if (was_stuck) stuck = true;  // stopped in an earlier launch: no more steps
         if (sflags & SEG_CORR) {
-            // The later batched passes' correction of this chain (x <- x - S^T z summed
-            // over the passes after the first, in FP32: it is what the first FP64 pass
-            // left, ~1e-4 of the residual's preimage).
+            // The batched passes' correction of this chain, x <- x - S^T z summed over
+            // the passes, held as a double-float pair: two FP64 subtractions per
+            // reaction (the FP32 -> FP64 conversions are integer operations).
 #pragma unroll
             for (int k = 0; k < EPT; ++k) {
                 const int i = tid + k * BD;
-                if (i < a.n) xs[i] -= (double)a.seg_dx[(size_t)p * (size_t)a.ld_seg + (size_t)i];
+                if (i < a.n) {
+                    const size_t o = (size_t)p * (size_t)a.ld_seg + (size_t)i;
+                    xs[i] = (xs[i] - f32_to_f64_exact(a.seg_dxh[o])) - f32_to_f64_exact(a.seg_dxl[o]);
+                }
             }
         }
         if (sflags & SEG_PENDING) {
@@ -1002,16 +1016,16 @@ __global__ void __launch_bounds__(BD, (BD <= 384 ? 2 : 1)) achr_chain_kernel(con
                         }
                         unsigned short *rh = a.seg_Rh + (size_t)p * (size_t)a.kpad;
                         unsigned short *rl = a.seg_Rl + (size_t)p * (size_t)a.kpad;
-                        float *r32 = a.seg_r + (size_t)p * (size_t)a.ld_r;
+                        double *rd = a.seg_rd + (size_t)p * (size_t)a.ld_r;
                         for (int q = tid; q < a.m; q += BD) {
-                            // (one FP64 conversion per row; the split itself is FP32)
-                            const float f = __double2float_rn(rr[q]);
+                            // (no FP64 operation: the FP32 image for the split is a truncation by
+                            // integer operations, and the FP64 value is stored as it is)
                             unsigned short h, l;
-                            split_bf16_bits(f, h, l);
+                            split_bf16_bits(f64_to_f32_rz(rr[q]), h, l);
                             const int row = __ldg(a.row_orig + q);
                             rh[row] = h;
                             rl[row] = l;
-                            r32[row] = f;
+                            rd[row] = rr[q];
                         }
                     }
 #pragma unroll

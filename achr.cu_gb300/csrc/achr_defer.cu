@@ -13,28 +13,34 @@
 // Here every chain runs to its next check step in one launch of the chain
 // kernel (segmented mode, achr_chain_kernel.cuh), which ends each chain right
 // after the check step's x <- x + t u and leaves, for every chain whose FP64
-// residual exceeds the tolerance, r = S x in FP32 and split into BF16 hi + lo
+// residual exceeds the tolerance, r = S x (FP64) and its BF16 hi + lo split
 // (chain-major block R).  The batched passes then apply the same orthogonal
 // projector to all of those chains at once,
 //
 //     x <- x - S^T z,   z = B r,   B = (S S^T)^+,
 //
 // z for every chain as one tensor-core GEMM Z = R B^T (three BF16 split
-// products, FP32 accumulation, achr_tc_gemm.cu).  The first pass applies
-// S^T z to the point in FP64 and recomputes the true residual S x in FP64, so
-// its update leaves the null-space part of x alone to FP64 rounding and what
-// is left of the residual is measured exactly (about 1e-4 of it on the
-// generator-law models).  Later passes only move the point by that remainder:
-// they form d = S^T z, add it to a correction dx and track r <- r - S d, all in
-// FP32, and the next launch subtracts dx from the point in FP64.  A chain takes
-// passes until max|r| falls to max(residual_tol / 100, 1e-7 of the residual its
-// check found), so the corrected point is within about 1e-7 of the
-// correction's own size of the FP64 projection; models whose S S^T has a
-// condition number above 2e4 reproject in the chain kernel instead.  The next
-// launch also clips the point and adds it to its centre accumulator before the
-// chain's next step, the order the reference uses.  The decisions (which
-// chains reproject) are the chain kernel's own FP64 residual, identical to the
-// check it makes when it reprojects in place.
+// products, FP32 accumulation, achr_tc_gemm.cu).  The first pass removes all
+// but ~1e-4 of the residual, so two things in it must be exact to FP64 level:
+// the update d = S^T z (any rounding outside the row space of S would move the
+// point off the reference's projection for good) and the new residual
+// r <- r - S d (later passes can only remove what they measure).  GB300's
+// FP64 pipe is the chain kernel's bottleneck, so both run in double-float
+// arithmetic on the FP32 pipes (values as unevaluated sums hi + lo of two
+// floats, error-free products and sums, about 48 significant bits).  Later
+// passes only move the point by what is left: they form d = S^T z in FP32,
+// add it into the double-float correction and track r in FP32.  The next
+// launch of the chain kernel subtracts the correction (two FP64 additions per
+// reaction), clips the point and adds it to its centre accumulator before the
+// chain's next step, the order the reference uses.  A chain takes passes
+// until max|r| falls to max(residual_tol / 1000, 1e-9 of the residual its
+// check found), which leaves the point within that, over the smallest singular
+// value of S, of the FP64 projection; models whose S S^T has a condition
+// number above 2e4 reproject in the chain kernel instead.  The decisions
+// (which chains reproject) are the chain kernel's own FP64 residual, identical
+// to the check it makes when it reprojects in place.  S and S^T are read as
+// sliced-ELL blocks (32 lines per group, slot-major, lines sorted by length)
+// so a warp's loads of one slot are one coalesced segment.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -50,19 +56,32 @@ extern "C" void achr_io_set_error(const char *msg);
 
 namespace achr {
 
+// Sparse lines (rows of S, or rows of S^T = columns of S) as a sliced-ELL
+// block: groups of 32 lines sorted by length, slot t of lane l of group g at
+// off[g] + 32 t + l, zero padding; values split into FP32 hi + lo.
+struct SlicedEll {
+    int groups = 0;
+    DevBuf<int> off;      // groups + 1
+    DevBuf<int> line;     // 32 * groups: the line lane l of group g holds (-1: none)
+    DevBuf<int> idx;      // the other index of each entry
+    DevBuf<float> vh, vl;
+};
+
 struct DeferState {
     int cap = 0;             // chains the buffers hold
     long long ld = 0;        // leading dimension of the chain-major state (n rounded up to even)
     int ldz = 0;             // leading dimension of Z and r (m rounded up to a multiple of 4)
     int kpad = 0;            // K of the GEMM: m rounded up to a multiple of 64
+    bool exact32 = false;    // every coefficient of S is exact in FP32 (all lo parts zero)
     DevBuf<double> x, A;     // cap x ld: points and centre accumulators between launches
     DevBuf<unsigned> flags;  // cap: SEG_* bits
     DevBuf<unsigned short> Rh, Rl;  // cap x kpad BF16 bits: S x of the chains that reproject
-    DevBuf<float> Z;         // cap x ldz: B (S x)
-    DevBuf<float> r;         // cap x ldz: S x in FP32, tracked through the passes
-    DevBuf<float> dx;        // cap x ld: the passes' summed correction S^T z
+    DevBuf<double> rd;       // cap x ldz: S x at the check, FP64
+    DevBuf<float> Z;         // cap x ldz: B r
+    DevBuf<float> r;         // cap x ldz: r after each pass, FP32
+    DevBuf<float> dxh, dxl;  // cap x ld: the passes' summed correction S^T z, double-float
     DevBuf<float> r0;        // cap: max|S x| of the chain when its check fired
-    DevBuf<float> cv32, rv32;  // CSC and CSR values of S in FP32 (model row order)
+    SlicedEll cols, rows;    // S^T and S, model row order
     DevBuf<int> row_orig;    // m: device row order of S -> the model's row order
     DevBuf<unsigned long long> any;  // one word per launch and pass: some chain needs that pass
     int any_cap = 0;
@@ -82,12 +101,13 @@ namespace {
 
 constexpr int kDeferChunk = 131072;        // chains per sweep through the segments (bounds the buffers)
 constexpr double kDeferMaxKappa = 2.0e4;   // largest condition number of S S^T the passes are used for
-constexpr int kCorrThreads = 256;
+constexpr int kPassThreads = 256;
+constexpr int kPassWarps = kPassThreads / 32;
 constexpr int kMaxPasses = 8;              // passes of one deferred reprojection at most
-// A chain's passes end once max|S x| <= max(residual_tol / 100, kRelTol times the residual its
-// check found): the point is then within about that fraction of the correction's size of the
-// FP64 projection (the correction is the residual's preimage).
-constexpr float kRelTol = 1e-7f;
+// A chain's passes end once max|S x| <= max(residual_tol / 1000, kRelTol times the residual its
+// check found): the point is then within that, over the smallest singular value of S, of the
+// FP64 projection.
+constexpr float kRelTol = 1e-9f;
 
 achr_status set_err(achr_status st, const std::string &msg) {
     achr_io_set_error(msg.c_str());
@@ -100,176 +120,288 @@ achr_status set_err(achr_status st, const std::string &msg) {
         if (e_ != cudaSuccess) return set_err(ACHR_ERR_CUDA, std::string(#expr) + ": " + cudaGetErrorString(e_)); \
     } while (0)
 
-__global__ void to_f32_kernel(long long count, const double *__restrict__ in, float *__restrict__ out) {
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t < count) out[t] = __double2float_rn(in[t]);
+// Error-free transformations on FP32 (IEEE round-to-nearest; nvcc neither
+// reassociates these nor contracts them beyond the explicit fmaf).
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+    s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+__device__ __forceinline__ void fast_two_sum(float a, float b, float &s, float &e) {  // |a| >= |b| or a = 0
+    s = __fadd_rn(a, b);
+    e = __fsub_rn(b, __fsub_rn(s, a));
+}
+__device__ __forceinline__ void two_prod(float a, float b, float &p, float &e) {
+    p = __fmul_rn(a, b);
+    e = fmaf(a, b, -p);
 }
 
-// The first pass, in FP64, for every chain flagged SEG_REPROJ (a CTA per chain
-// at a time, chain-major rows): x <- x - S^T z1 and r1 = S x, both FP64, with z1
-// the GEMM's row of that chain.  This pass removes nearly all of the residual
-// (what is left is ~1e-4 of it), so its update must not leak into the null
-// space and r1 must be the true residual of the new point: both are FP64 here,
-// and the later passes, which only move the point by what is left, run in FP32.
-// r1 goes to Rf (FP32) and R (BF16 hi/lo); max|r| of the chain's check (from
-// Rf before the update) to r0; convergence as in defer_pass_kernel.
-__global__ void __launch_bounds__(kCorrThreads)
-    defer_first_pass_kernel(int n, int m, int kpad, int P, unsigned *__restrict__ flags, const float *__restrict__ Z,
-                            float *__restrict__ Rf, long long ldz, double *__restrict__ X, long long ldx,
-                            float *__restrict__ r0, const int *__restrict__ cp, const int *__restrict__ ri,
-                            const double *__restrict__ cv, const int *__restrict__ rp, const int *__restrict__ ci,
-                            const double *__restrict__ rv, __nv_bfloat16 *__restrict__ Rh,
-                            __nv_bfloat16 *__restrict__ Rl, float fine_tol, float rel_tol, float residual_tol,
-                            int last, const unsigned long long *this_gate, unsigned long long *next_any,
-                            unsigned long long *counters) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    __shared__ float wmax[kCorrThreads / 32][2];
-    double *zd = reinterpret_cast<double *>(smem_raw);
-    double *xs = zd + ldz;
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    if (*this_gate == 0ull) return;  // no chain's check fired (the GEMM did not run either)
-    if (blockIdx.x == 0 && tid == 0) atomicAdd(counters + CNT_GEMMS, 1ull);
-    for (int p = blockIdx.x; p < P; p += gridDim.x) {
-        if (!(flags[p] & SEG_REPROJ)) continue;  // uniform over the block
-        const float *zp = Z + (size_t)p * (size_t)ldz;
-        float *rp_ = Rf + (size_t)p * (size_t)ldz;
-        float m0 = 0.0f;
-        for (int i = tid; i < m; i += kCorrThreads) {
-            zd[i] = (double)zp[i];
-            m0 = fmaxf(m0, fabsf(rp_[i]));
-        }
-        __syncthreads();
-        double *xp = X + (size_t)p * (size_t)ldx;
-        for (int j = tid; j < n; j += kCorrThreads) {
-            double dl = 0.0;
-            const int q1 = __ldg(cp + j + 1);
-            for (int q = __ldg(cp + j); q < q1; ++q) dl = fma(__ldg(cv + q), zd[__ldg(ri + q)], dl);
-            const double xv = xp[j] - dl;
-            xp[j] = xv;
-            xs[j] = xv;
-        }
-        __syncthreads();
-        __nv_bfloat16 *rh = Rh + (size_t)p * (size_t)kpad, *rl = Rl + (size_t)p * (size_t)kpad;
-        float mx = 0.0f;
-        for (int i = tid; i < m; i += kCorrThreads) {
-            double acc = 0.0;
-            const int q1 = __ldg(rp + i + 1);
-            for (int q = __ldg(rp + i); q < q1; ++q) acc = fma(__ldg(rv + q), xs[__ldg(ci + q)], acc);
-            const float rn = __double2float_rn(acc);
-            rp_[i] = rn;
-            mx = fmaxf(mx, fabsf(rn));
-            if (!last) {
-                const __nv_bfloat16 hi = __float2bfloat16_rn(rn);
-                rh[i] = hi;
-                rl[i] = __float2bfloat16_rn(rn - __bfloat162float(hi));
-            }
-        }
-#pragma unroll
-        for (int o = 16; o; o >>= 1) {
-            mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-            m0 = fmaxf(m0, __shfl_xor_sync(0xffffffffu, m0, o));
-        }
-        if (lane == 0) {
-            wmax[warp][0] = mx;
-            wmax[warp][1] = m0;
-        }
-        __syncthreads();
-        if (tid == 0) {
-            for (int w = 1; w < kCorrThreads / 32; ++w) {
-                mx = fmaxf(mx, wmax[w][0]);
-                m0 = fmaxf(m0, wmax[w][1]);
-            }
-            atomicAdd(counters + CNT_PASSES, 1ull);
-            r0[p] = m0;  // the residual the chain's check found
-            if (mx <= fmaxf(fine_tol, rel_tol * m0)) {
-                flags[p] &= ~SEG_REPROJ;  // converged
-            } else if (!last) {
-                if (*next_any == 0ull) atomicOr(next_any, 1ull);
-            } else if (mx > residual_tol) {
-                atomicOr(counters + CNT_ERROR, (unsigned long long)ERR_DEFER_DIVERGED);
-            }
-        }
-        __syncthreads();
+// FP64 -> (hi, lo) FP32 with integer operations only: hi is v truncated to 24
+// significant bits, lo the rest (up to 29 bits, rounded to 24); |v - hi - lo|
+// <= 2^-48 |v|.  Values below 2^-126 become 0.
+__device__ __forceinline__ void split_f64(double v, float &hi, float &lo) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+    const unsigned sign = (unsigned)(b >> 32) & 0x80000000u;
+    const int e = (int)((b >> 52) & 0x7FF);
+    const int fe = e - 896;  // FP32 biased exponent
+    if (fe <= 0 || fe >= 255) {
+        hi = (fe >= 255) ? __uint_as_float(sign | 0x7F800000u) : __uint_as_float(sign);
+        lo = 0.0f;
+        return;
+    }
+    const unsigned long long mant = b & 0xFFFFFFFFFFFFFull;
+    hi = __uint_as_float(sign | ((unsigned)fe << 23) | (unsigned)(mant >> 29));
+    const unsigned rest = (unsigned)(mant & 0x1FFFFFFFull);  // the low 29 bits: rest * 2^(e - 1075)
+    const float r = __uint2float_rn(rest);
+    const float l = ldexpf(r, e - 1075);
+    lo = sign ? -l : l;
+}
+
+__device__ __forceinline__ void split_store(float r, __nv_bfloat16 *rh, __nv_bfloat16 *rl, int i) {
+    const __nv_bfloat16 h = __float2bfloat16_rn(r);
+    rh[i] = h;
+    rl[i] = __float2bfloat16_rn(__fsub_rn(r, __bfloat162float(h)));
+}
+
+struct EllView {
+    int groups;
+    const int *off, *line, *idx;
+    const float *vh, *vl;
+};
+
+struct PassArgs {
+    int n, m, kpad, P, pass, last;
+    long long ld, ldz;
+    unsigned *flags;
+    const float *Z;
+    const double *rd;
+    float *r, *dxh, *dxl, *r0;
+    __nv_bfloat16 *Rh, *Rl;
+    EllView cols, rows;  // S^T (lines = columns of S) and S (lines = rows of S)
+    float fine_tol, rel_tol, residual_tol;
+    const unsigned long long *this_gate;
+    unsigned long long *next_any, *counters;
+};
+
+// End of a chain's pass (thread 0): convergence, next-pass gate, divergence.
+__device__ __forceinline__ void pass_verdict(const PassArgs &a, int p, float mx, float r0max) {
+    atomicAdd(a.counters + CNT_PASSES, 1ull);
+    if (mx <= fmaxf(a.fine_tol, a.rel_tol * r0max)) {
+        a.flags[p] &= ~SEG_REPROJ;  // converged
+    } else if (!a.last) {
+        if (*a.next_any == 0ull) atomicOr(a.next_any, 1ull);
+    } else if (mx > a.residual_tol) {
+        atomicOr(a.counters + CNT_ERROR, (unsigned long long)ERR_DEFER_DIVERGED);
     }
 }
 
-// A later pass (pass >= 1) for every chain still flagged SEG_REPROJ (a CTA
-// per chain at a time; chain-major rows, so every load and store is coalesced):
-//     d = S^T z,  dx += d,  r <- r - S d,
-// z the chain's row of the GEMM's B r.  Everything here is FP32: after the
-// first pass the residual is ~1e-4 of what the check found, d is of that size,
-// and r is tracked from the first pass's FP64 residual, so FP32 rounding stays
-// relative to what is left, not to x; the point is touched once, in FP64, when
-// the next launch subtracts dx (SEG_CORR).  A chain whose max|r| falls to
-// max(fine_tol, rel_tol max|r0|) is done (flag cleared); any other has r split
-// into R for the next pass and marks that pass as needed.  After the last pass
-// a chain still above residual_tol raises ERR_DEFER_DIVERGED.  S is read in the
-// model's row order (CSC for S^T z, CSR for S d), matching B.
-__global__ void __launch_bounds__(kCorrThreads)
-    defer_pass_kernel(int n, int m, int kpad, int P, int pass, unsigned *__restrict__ flags,
-                      const float *__restrict__ Z, float *__restrict__ Rf, long long ldz, float *__restrict__ DX,
-                      long long ldx, float *__restrict__ r0, const int *__restrict__ cp, const int *__restrict__ ri,
-                      const float *__restrict__ cv, const int *__restrict__ rp, const int *__restrict__ ci,
-                      const float *__restrict__ rv, __nv_bfloat16 *__restrict__ Rh, __nv_bfloat16 *__restrict__ Rl,
-                      float fine_tol, float rel_tol, float residual_tol, int last,
-                      const unsigned long long *this_gate, unsigned long long *next_any,
-                      unsigned long long *counters) {
+__device__ __forceinline__ float block_max(float v, float *red) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 16; o; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    if (lane == 0) red[warp] = v;
+    __syncthreads();
+    float m = red[0];
+#pragma unroll
+    for (int w = 1; w < kPassWarps; ++w) m = fmaxf(m, red[w]);
+    __syncthreads();
+    return m;
+}
+
+// The first pass for every chain flagged SEG_REPROJ (one CTA per chain at a
+// time), in double-float: d = S^T z (z the chain's GEMM row), dx = d, and
+// r = r0 - S d from the chain kernel's FP64 r0; r goes on in FP32 (Rf) and as
+// the next GEMM's BF16 split.
+template <bool EXACT32>
+__global__ void __launch_bounds__(kPassThreads) defer_pass1_kernel(const PassArgs a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    __shared__ float wmax[kCorrThreads / 32];
+    __shared__ float red[kPassWarps];
     float *zs = reinterpret_cast<float *>(smem_raw);
-    float *ds = zs + ldz;
+    float *dh = zs + a.ldz;
+    float *dl = dh + a.ld;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    if (*this_gate == 0ull) return;  // no chain needed this pass (its GEMM did not run either)
-    if (blockIdx.x == 0 && tid == 0) atomicAdd(counters + CNT_GEMMS, 1ull);
-    for (int p = blockIdx.x; p < P; p += gridDim.x) {
-        if (!(flags[p] & SEG_REPROJ)) continue;  // uniform over the block
-        const float *zp = Z + (size_t)p * (size_t)ldz;
-        for (int i = tid; i < m; i += kCorrThreads) zs[i] = zp[i];
+    if (*a.this_gate == 0ull) return;  // no chain's check fired (the GEMM did not run either)
+    if (blockIdx.x == 0 && tid == 0) atomicAdd(a.counters + CNT_GEMMS, 1ull);
+    for (int p = blockIdx.x; p < a.P; p += gridDim.x) {
+        if (!(a.flags[p] & SEG_REPROJ)) continue;  // uniform over the block
+        const float *zp = a.Z + (size_t)p * (size_t)a.ldz;
+        for (int i = tid; i < a.m; i += kPassThreads) zs[i] = zp[i];
         __syncthreads();
-        float *dxp = DX + (size_t)p * (size_t)ldx;
-        for (int j = tid; j < n; j += kCorrThreads) {
-            float dl = 0.0f;
-            const int q1 = __ldg(cp + j + 1);
-            for (int q = __ldg(cp + j); q < q1; ++q) dl = fmaf(__ldg(cv + q), zs[__ldg(ri + q)], dl);
-            ds[j] = dl;
-            dxp[j] = pass == 1 ? dl : dxp[j] + dl;
-        }
-        __syncthreads();
-        float *rp_ = Rf + (size_t)p * (size_t)ldz;
-        __nv_bfloat16 *rh = Rh + (size_t)p * (size_t)kpad, *rl = Rl + (size_t)p * (size_t)kpad;
-        float mx = 0.0f;
-        for (int i = tid; i < m; i += kCorrThreads) {
-            const float ro = rp_[i];
-            float acc = 0.0f;
-            const int q1 = __ldg(rp + i + 1);
-            for (int q = __ldg(rp + i); q < q1; ++q) acc = fmaf(__ldg(rv + q), ds[__ldg(ci + q)], acc);
-            const float rn = ro - acc;
-            rp_[i] = rn;
-            mx = fmaxf(mx, fabsf(rn));
-            if (!last) {
-                const __nv_bfloat16 hi = __float2bfloat16_rn(rn);
-                rh[i] = hi;
-                rl[i] = __float2bfloat16_rn(rn - __bfloat162float(hi));
+        float *dxh = a.dxh + (size_t)p * (size_t)a.ld, *dxl = a.dxl + (size_t)p * (size_t)a.ld;
+        for (int g = warp; g < a.cols.groups; g += kPassWarps) {
+            const int base = __ldg(a.cols.off + g);
+            const int len = (__ldg(a.cols.off + g + 1) - base) >> 5;
+            float ah = 0.0f, al = 0.0f;
+#pragma unroll 4
+            for (int t = 0; t < len; ++t) {
+                const int q = base + (t << 5) + lane;
+                const float z = zs[__ldg(a.cols.idx + q)];
+                float ph, pe, s, e;
+                two_prod(__ldg(a.cols.vh + q), z, ph, pe);
+                if (!EXACT32) pe = fmaf(__ldg(a.cols.vl + q), z, pe);
+                two_sum(ah, ph, s, e);
+                ah = s;
+                al = __fadd_rn(al, __fadd_rn(e, pe));
+            }
+            float h, l;
+            fast_two_sum(ah, al, h, l);
+            const int j = __ldg(a.cols.line + (g << 5) + lane);
+            if (j >= 0) {
+                dh[j] = h;
+                dl[j] = l;
+                dxh[j] = h;
+                dxl[j] = l;
             }
         }
-#pragma unroll
-        for (int o = 16; o; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-        if (lane == 0) wmax[warp] = mx;
         __syncthreads();
+        const double *rdp = a.rd + (size_t)p * (size_t)a.ldz;
+        float *rp = a.r + (size_t)p * (size_t)a.ldz;
+        __nv_bfloat16 *rh = a.Rh + (size_t)p * (size_t)a.kpad, *rl = a.Rl + (size_t)p * (size_t)a.kpad;
+        float mx = 0.0f, m0 = 0.0f;
+        for (int g = warp; g < a.rows.groups; g += kPassWarps) {
+            const int i = __ldg(a.rows.line + (g << 5) + lane);
+            float ah = 0.0f, al = 0.0f;
+            if (i >= 0) split_f64(rdp[i], ah, al);
+            m0 = fmaxf(m0, fabsf(ah));
+            const int base = __ldg(a.rows.off + g);
+            const int len = (__ldg(a.rows.off + g + 1) - base) >> 5;
+#pragma unroll 4
+            for (int t = 0; t < len; ++t) {
+                const int q = base + (t << 5) + lane;
+                const int j = __ldg(a.rows.idx + q);
+                const float sh = __ldg(a.rows.vh + q);
+                const float xh = dh[j], xl = dl[j];
+                float ph, pe, s, e;
+                two_prod(sh, xh, ph, pe);
+                pe = fmaf(sh, xl, pe);
+                if (!EXACT32) pe = fmaf(__ldg(a.rows.vl + q), xh, pe);
+                two_sum(ah, -ph, s, e);
+                ah = s;
+                al = __fadd_rn(al, __fsub_rn(e, pe));
+            }
+            if (i >= 0) {
+                const float rn = __fadd_rn(ah, al);
+                rp[i] = rn;
+                mx = fmaxf(mx, fabsf(rn));
+                if (!a.last) split_store(rn, rh, rl, i);
+            }
+        }
+        mx = block_max(mx, red);
+        m0 = block_max(m0, red);
         if (tid == 0) {
-            for (int w = 1; w < kCorrThreads / 32; ++w) mx = fmaxf(mx, wmax[w]);
-            atomicAdd(counters + CNT_PASSES, 1ull);
-            if (pass == 1) flags[p] |= SEG_CORR;  // dx now holds a correction for the next launch
-            if (mx <= fmaxf(fine_tol, rel_tol * r0[p])) {
-                flags[p] &= ~SEG_REPROJ;  // converged
-            } else if (!last) {
-                if (*next_any == 0ull) atomicOr(next_any, 1ull);
-            } else if (mx > residual_tol) {
-                atomicOr(counters + CNT_ERROR, (unsigned long long)ERR_DEFER_DIVERGED);
-            }
+            a.flags[p] |= SEG_CORR;  // dx holds a correction for the next launch
+            a.r0[p] = m0;
+            pass_verdict(a, p, mx, m0);
         }
         __syncthreads();
     }
+}
+
+// A later pass (pass >= 1) for every chain still flagged SEG_REPROJ, in FP32:
+// d = S^T z, dx += d (double-float), r <- r - S d.
+__global__ void __launch_bounds__(kPassThreads) defer_pass_kernel(const PassArgs a) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ float red[kPassWarps];
+    float *zs = reinterpret_cast<float *>(smem_raw);
+    float *ds = zs + a.ldz;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (*a.this_gate == 0ull) return;  // no chain needed this pass (its GEMM did not run either)
+    if (blockIdx.x == 0 && tid == 0) atomicAdd(a.counters + CNT_GEMMS, 1ull);
+    for (int p = blockIdx.x; p < a.P; p += gridDim.x) {
+        if (!(a.flags[p] & SEG_REPROJ)) continue;  // uniform over the block
+        const float *zp = a.Z + (size_t)p * (size_t)a.ldz;
+        for (int i = tid; i < a.m; i += kPassThreads) zs[i] = zp[i];
+        __syncthreads();
+        float *dxh = a.dxh + (size_t)p * (size_t)a.ld, *dxl = a.dxl + (size_t)p * (size_t)a.ld;
+        for (int g = warp; g < a.cols.groups; g += kPassWarps) {
+            const int base = __ldg(a.cols.off + g);
+            const int len = (__ldg(a.cols.off + g + 1) - base) >> 5;
+            float d = 0.0f;
+#pragma unroll 4
+            for (int t = 0; t < len; ++t) {
+                const int q = base + (t << 5) + lane;
+                d = fmaf(__ldg(a.cols.vh + q), zs[__ldg(a.cols.idx + q)], d);
+            }
+            const int j = __ldg(a.cols.line + (g << 5) + lane);
+            if (j >= 0) {
+                ds[j] = d;
+                float s, e;
+                two_sum(dxh[j], d, s, e);
+                dxh[j] = s;
+                dxl[j] = __fadd_rn(dxl[j], e);
+            }
+        }
+        __syncthreads();
+        float *rp = a.r + (size_t)p * (size_t)a.ldz;
+        __nv_bfloat16 *rh = a.Rh + (size_t)p * (size_t)a.kpad, *rl = a.Rl + (size_t)p * (size_t)a.kpad;
+        float mx = 0.0f;
+        for (int g = warp; g < a.rows.groups; g += kPassWarps) {
+            const int base = __ldg(a.rows.off + g);
+            const int len = (__ldg(a.rows.off + g + 1) - base) >> 5;
+            float acc = 0.0f;
+#pragma unroll 4
+            for (int t = 0; t < len; ++t) {
+                const int q = base + (t << 5) + lane;
+                acc = fmaf(__ldg(a.rows.vh + q), ds[__ldg(a.rows.idx + q)], acc);
+            }
+            const int i = __ldg(a.rows.line + (g << 5) + lane);
+            if (i >= 0) {
+                const float rn = __fsub_rn(rp[i], acc);
+                rp[i] = rn;
+                mx = fmaxf(mx, fabsf(rn));
+                if (!a.last) split_store(rn, rh, rl, i);
+            }
+        }
+        mx = block_max(mx, red);
+        if (tid == 0) pass_verdict(a, p, mx, a.r0[p]);
+        __syncthreads();
+    }
+}
+
+// Sliced-ELL block of the lines of a sparse matrix given as CSR-like
+// (ptr, idx, val) over n_lines lines; lines sorted by length, longest first.
+achr_status build_ell(SlicedEll &E, int n_lines, const std::vector<int> &ptr, const std::vector<int> &idx,
+                      const std::vector<double> &val, bool &exact32) {
+    std::vector<int> order((size_t)n_lines);
+    for (int l = 0; l < n_lines; ++l) order[(size_t)l] = l;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+        return ptr[(size_t)a + 1] - ptr[(size_t)a] > ptr[(size_t)b + 1] - ptr[(size_t)b];
+    });
+    const int groups = (n_lines + 31) / 32;
+    std::vector<int> off((size_t)groups + 1, 0), line((size_t)groups * 32, -1), eidx;
+    std::vector<float> vh, vl;
+    for (int g = 0; g < groups; ++g) {
+        int len = 0;
+        for (int l = 0; l < 32 && 32 * g + l < n_lines; ++l) {
+            const int L = order[(size_t)(32 * g + l)];
+            line[(size_t)(32 * g + l)] = L;
+            len = std::max(len, ptr[(size_t)L + 1] - ptr[(size_t)L]);
+        }
+        off[(size_t)g + 1] = off[(size_t)g] + 32 * len;
+        for (int t = 0; t < len; ++t)
+            for (int l = 0; l < 32; ++l) {
+                const int L = line[(size_t)(32 * g + l)];
+                const bool real = L >= 0 && t < ptr[(size_t)L + 1] - ptr[(size_t)L];
+                const double v = real ? val[(size_t)ptr[(size_t)L] + t] : 0.0;
+                const float h = (float)v;
+                const float lo = (float)(v - (double)h);
+                if (lo != 0.0f) exact32 = false;
+                eidx.push_back(real ? idx[(size_t)ptr[(size_t)L] + t] : 0);
+                vh.push_back(h);
+                vl.push_back(lo);
+            }
+    }
+    E.groups = groups;
+    DEFER_TRY(E.off.upload(off.data(), off.size()));
+    DEFER_TRY(E.line.upload(line.data(), line.size()));
+    DEFER_TRY(E.idx.upload(eidx.data(), eidx.size()));
+    DEFER_TRY(E.vh.upload(vh.data(), vh.size()));
+    DEFER_TRY(E.vl.upload(vl.data(), vl.size()));
+    return ACHR_OK;
+}
+
+EllView view(const SlicedEll &E) {
+    return EllView{E.groups, E.off.p, E.line.p, E.idx.p, E.vh.p, E.vl.p};
 }
 
 achr_status ensure_defer(achr_ctx *ctx, int chains, int segments) {
@@ -283,13 +415,29 @@ achr_status ensure_defer(achr_ctx *ctx, int chains, int segments) {
         D->ld = (ctx->n + 1) & ~1;
         D->ldz = (ctx->m + 3) & ~3;
         DEFER_TRY(D->row_orig.upload(ctx->h_row_order.data(), ctx->h_row_order.size()));
-        const long long nnz = (long long)R.cv.count;
-        DEFER_TRY(D->cv32.alloc((size_t)nnz));
-        DEFER_TRY(D->rv32.alloc((size_t)nnz));
-        to_f32_kernel<<<(unsigned)((nnz + 255) / 256), 256>>>(nnz, R.cv.p, D->cv32.p);
-        to_f32_kernel<<<(unsigned)((nnz + 255) / 256), 256>>>(nnz, R.rv.p, D->rv32.p);
-        DEFER_TRY(cudaGetLastError());
-        DEFER_TRY(cudaDeviceSynchronize());
+        // S (rows) and S^T (columns of S) in the model's row order, the order of B's rows.
+        const int n = ctx->n, m = ctx->m;
+        const std::vector<int> &rp = ctx->h_rowptr, &ci = ctx->h_colidx;
+        const std::vector<double> &rv = ctx->h_val;
+        std::vector<int> cp((size_t)n + 1, 0), ri(ci.size());
+        std::vector<double> cv(ci.size());
+        for (int c : ci) cp[(size_t)c + 1]++;
+        for (int j = 0; j < n; ++j) cp[(size_t)j + 1] += cp[(size_t)j];
+        {
+            std::vector<int> fill(cp.begin(), cp.end() - 1);
+            for (int i = 0; i < m; ++i)
+                for (int q = rp[(size_t)i]; q < rp[(size_t)i + 1]; ++q) {
+                    const int dst = fill[(size_t)ci[(size_t)q]]++;
+                    ri[(size_t)dst] = i;
+                    cv[(size_t)dst] = rv[(size_t)q];
+                }
+        }
+        bool exact = true;
+        achr_status st = build_ell(D->cols, n, cp, ri, cv, exact);
+        if (st != ACHR_OK) return st;
+        st = build_ell(D->rows, m, rp, ci, rv, exact);
+        if (st != ACHR_OK) return st;
+        D->exact32 = exact;
     }
     if (D->cap < chains) {
         D->cap = 0;
@@ -302,9 +450,11 @@ achr_status ensure_defer(achr_ctx *ctx, int chains, int segments) {
         // the K padding of R (rows m..kpad) is never written and must be zero
         DEFER_TRY(cudaMemset(D->Rh.p, 0, sizeof(unsigned short) * c * (size_t)D->kpad));
         DEFER_TRY(cudaMemset(D->Rl.p, 0, sizeof(unsigned short) * c * (size_t)D->kpad));
+        DEFER_TRY(D->rd.alloc(c * (size_t)D->ldz));
         DEFER_TRY(D->Z.alloc(c * (size_t)D->ldz));
         DEFER_TRY(D->r.alloc(c * (size_t)D->ldz));
-        DEFER_TRY(D->dx.alloc(c * (size_t)D->ld));
+        DEFER_TRY(D->dxh.alloc(c * (size_t)D->ld));
+        DEFER_TRY(D->dxl.alloc(c * (size_t)D->ld));
         DEFER_TRY(D->r0.alloc(c));
         D->cap = chains;
     }
@@ -358,20 +508,18 @@ achr_status defer_sample(achr_ctx *ctx, const ChainArgs &a_in, int threads_per_c
         return cudaEventRecord(D.ev[(size_t)D.ev_used++], s);
     };
     const int passes = ctx->opt.reprojection_passes > 0 ? ctx->opt.reprojection_passes : kMaxPasses;
-    const double fine_tol = ctx->opt.residual_tol * 0.01;
+    const double fine_tol = ctx->opt.residual_tol * 1e-3;
 
-    int dev = 0, sms = 0, per_sm = 0;
+    int dev = 0, sms = 0, per_sm = 0, per_sm1 = 0;
     DEFER_TRY(cudaGetDevice(&dev));
     DEFER_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    const size_t corr_smem = sizeof(float) * ((size_t)D.ldz + (size_t)D.ld);
-    const size_t first_smem = sizeof(double) * ((size_t)D.ldz + (size_t)D.ld);
-    int per_sm1 = 0;
-    DEFER_TRY(cudaFuncSetAttribute(defer_pass_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)corr_smem));
-    DEFER_TRY(cudaFuncSetAttribute(defer_first_pass_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)first_smem));
-    DEFER_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, defer_pass_kernel, kCorrThreads, corr_smem));
-    DEFER_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm1, defer_first_pass_kernel, kCorrThreads,
-                                                            first_smem));
+    const size_t pass_smem = sizeof(float) * ((size_t)D.ldz + (size_t)D.ld);
+    const size_t pass1_smem = sizeof(float) * ((size_t)D.ldz + 2 * (size_t)D.ld);
+    auto *const pass1 = D.exact32 ? defer_pass1_kernel<true> : defer_pass1_kernel<false>;
+    DEFER_TRY(cudaFuncSetAttribute(defer_pass_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pass_smem));
+    DEFER_TRY(cudaFuncSetAttribute(pass1, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pass1_smem));
+    DEFER_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, defer_pass_kernel, kPassThreads, pass_smem));
+    DEFER_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm1, pass1, kPassThreads, pass1_smem));
     if (per_sm < 1 || per_sm1 < 1)
         return set_err(ACHR_ERR_UNSUPPORTED, "model too large for the batched reprojection's update");
 
@@ -398,11 +546,34 @@ achr_status defer_sample(achr_ctx *ctx, const ChainArgs &a_in, int threads_per_c
         a.seg_Rh = D.Rh.p;
         a.seg_Rl = D.Rl.p;
         a.kpad = D.kpad;
-        a.seg_r = D.r.p;
+        a.seg_rd = D.rd.p;
         a.ld_r = D.ldz;
-        a.seg_dx = D.dx.p;
-        const int corr_grid = (int)std::min<long long>((long long)sms * per_sm, pc);
-        const int first_grid = (int)std::min<long long>((long long)sms * per_sm1, pc);
+        a.seg_dxh = D.dxh.p;
+        a.seg_dxl = D.dxl.p;
+        const int pass_grid = (int)std::min<long long>((long long)sms * per_sm, pc);
+        const int pass1_grid = (int)std::min<long long>((long long)sms * per_sm1, pc);
+        PassArgs pa{};
+        pa.n = ctx->n;
+        pa.m = ctx->m;
+        pa.kpad = D.kpad;
+        pa.P = pc;
+        pa.ld = D.ld;
+        pa.ldz = D.ldz;
+        pa.flags = D.flags.p;
+        pa.Z = D.Z.p;
+        pa.rd = D.rd.p;
+        pa.r = D.r.p;
+        pa.dxh = D.dxh.p;
+        pa.dxl = D.dxl.p;
+        pa.r0 = D.r0.p;
+        pa.Rh = reinterpret_cast<__nv_bfloat16 *>(D.Rh.p);
+        pa.Rl = reinterpret_cast<__nv_bfloat16 *>(D.Rl.p);
+        pa.cols = view(D.cols);
+        pa.rows = view(D.rows);
+        pa.fine_tol = (float)fine_tol;
+        pa.rel_tol = kRelTol;
+        pa.residual_tol = (float)ctx->opt.residual_tol;
+        pa.counters = a_in.counters;
         int s0 = S0, seg = 0;
         for (;;) {
             // The launch runs to the first check step at or after s0 (the reference
@@ -427,19 +598,12 @@ achr_status defer_sample(achr_ctx *ctx, const ChainArgs &a_in, int threads_per_c
                 g.gate_max = 0;
                 if (const char *why = tc_gemm_check(g)) return set_err(ACHR_ERR_INVALID, why);
                 DEFER_TRY(launch_tc_gemm(g, a_in.counters + CNT_ERROR, s));
-                if (pass == 0)
-                    defer_first_pass_kernel<<<(unsigned)first_grid, kCorrThreads, first_smem, s>>>(
-                        ctx->n, ctx->m, R.kpad, pc, D.flags.p, D.Z.p, D.r.p, D.ldz, D.x.p, D.ld, D.r0.p, R.cp.p,
-                        R.ri.p, R.cv.p, R.rp.p, R.ci.p, R.rv.p, reinterpret_cast<__nv_bfloat16 *>(D.Rh.p),
-                        reinterpret_cast<__nv_bfloat16 *>(D.Rl.p), (float)fine_tol, kRelTol,
-                        (float)ctx->opt.residual_tol, passes == 1 ? 1 : 0, gate, gate + 1, a_in.counters);
-                else
-                    defer_pass_kernel<<<(unsigned)corr_grid, kCorrThreads, corr_smem, s>>>(
-                        ctx->n, ctx->m, R.kpad, pc, pass, D.flags.p, D.Z.p, D.r.p, D.ldz, D.dx.p, D.ld, D.r0.p,
-                        R.cp.p, R.ri.p, D.cv32.p, R.rp.p, R.ci.p, D.rv32.p,
-                        reinterpret_cast<__nv_bfloat16 *>(D.Rh.p), reinterpret_cast<__nv_bfloat16 *>(D.Rl.p),
-                        (float)fine_tol, kRelTol, (float)ctx->opt.residual_tol, pass + 1 == passes ? 1 : 0,
-                        gate + pass, gate + pass + 1, a_in.counters);
+                pa.pass = pass;
+                pa.last = pass + 1 == passes ? 1 : 0;
+                pa.this_gate = gate + pass;
+                pa.next_any = gate + pass + 1;
+                if (pass == 0) pass1<<<(unsigned)pass1_grid, kPassThreads, pass1_smem, s>>>(pa);
+                else defer_pass_kernel<<<(unsigned)pass_grid, kPassThreads, pass_smem, s>>>(pa);
                 DEFER_TRY(cudaGetLastError());
                 ctx->last_launches += 2;
             }

@@ -99,9 +99,9 @@ struct ChainArgs {
     const int *row_orig;           // device row q of S -> row in the model's order
     unsigned short *seg_Rh, *seg_Rl;  // P x kpad BF16 bits: hi and lo parts of S x
     int kpad;
-    float *seg_r;                  // P x ld_r: S x in FP32 (the batched passes track it from here)
+    double *seg_rd;                // P x ld_r: S x at the check (FP64), rows in the model's order
     long long ld_r;
-    const float *seg_dx;           // P x ld_seg: the batched passes' correction, subtracted at the next launch
+    const float *seg_dxh, *seg_dxl;  // P x ld_seg: the passes' correction (double-float), subtracted next launch
 };
 
 // Per-chain state bits of segmented sampling.

@@ -94,12 +94,13 @@ typedef struct {
                                     and the chains whose residual exceeds residual_tol are reprojected
                                     together, x <- x - S^T (S S^T)^+ S x with S x and the update in FP64
                                     and the dense product on the tensor cores (three BF16 split
-                                    products); the first pass updates the point in FP64, later ones
-                                    (FP32, on what is left) run per chain until max|S x| <=
-                                    max(residual_tol / 100, 1e-7 of the residual the check found); then
-                                    the clip and the centre update of that step, as the reference orders
-                                    them; needs n_mets <= the chain kernel's padded length and a condition
-                                    number of S S^T <= 2e4 (achr_sample,
+                                    products); the first pass's update S^T z and new residual are
+                                    exact to double-float (~48 bits), later ones (FP32, on what is left)
+                                    run per chain until max|S x| <= max(residual_tol / 1000, 1e-9 of the
+                                    residual the check found); then the clip and the centre update of
+                                    that step, as the reference orders them; needs n_mets <= the chain
+                                    kernel's padded length and a condition number of S S^T <= 2e4
+                                    (achr_sample,
                                     achr_sample_device and achr_sample_resume; batched launches
                                     reproject in the chain kernel, and so does choice 0 with a
                                     hit-and-run pool) */
