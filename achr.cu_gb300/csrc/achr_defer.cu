@@ -33,9 +33,9 @@
 // launch of the chain kernel subtracts the correction (two FP64 additions per
 // reaction), clips the point and adds it to its centre accumulator before the
 // chain's next step, the order the reference uses.  A chain takes passes
-// until max|r| falls to max(residual_tol / 1000, 1e-9 of the residual its
-// check found), which leaves the point within that, over the smallest singular
-// value of S, of the FP64 projection; models whose S S^T has a condition
+// until max|r| falls to residual_tol / 1000, which leaves the point within
+// that, over the smallest singular value of S, of the FP64 projection (about
+// the projection's own FP64 rounding); models whose S S^T has a condition
 // number above 2e4 reproject in the chain kernel instead.  The decisions
 // (which chains reproject) are the chain kernel's own FP64 residual, identical
 // to the check it makes when it reprojects in place.  S and S^T are read as
@@ -63,7 +63,7 @@ struct SlicedEll {
     int groups = 0;
     DevBuf<int> off;      // groups + 1
     DevBuf<int> line;     // 32 * groups: the line lane l of group g holds (-1: none)
-    DevBuf<int> idx;      // the other index of each entry
+    DevBuf<unsigned short> idx;  // the other index of each entry (n and m are below 65536)
     DevBuf<float> vh, vl;
 };
 
@@ -101,13 +101,15 @@ namespace {
 
 constexpr int kDeferChunk = 131072;        // chains per sweep through the segments (bounds the buffers)
 constexpr double kDeferMaxKappa = 2.0e4;   // largest condition number of S S^T the passes are used for
-constexpr int kPassThreads = 256;
+constexpr int kPassThreads = 512;
 constexpr int kPassWarps = kPassThreads / 32;
 constexpr int kMaxPasses = 8;              // passes of one deferred reprojection at most
-// A chain's passes end once max|S x| <= max(residual_tol / 1000, kRelTol times the residual its
-// check found): the point is then within that, over the smallest singular value of S, of the
-// FP64 projection.
-constexpr float kRelTol = 1e-9f;
+// A chain's passes end once max|S x| <= residual_tol / 1000 (1e-12 by default, about the FP64
+// rounding floor of S x for fluxes of size 1000): the point is then within that, over the
+// smallest singular value of S, of the FP64 projection.  (The bound is absolute: a check can
+// find a residual of 0.1 after 25 steps on %f warmups, and 1e-9 of that would still be 1e-10.)
+constexpr float kRelTol = 0.0f;
+constexpr size_t kPassSmemMax = 220 * 1024;  // dynamic shared memory a pass CTA may use
 
 achr_status set_err(achr_status st, const std::string &msg) {
     achr_io_set_error(msg.c_str());
@@ -165,7 +167,8 @@ __device__ __forceinline__ void split_store(float r, __nv_bfloat16 *rh, __nv_bfl
 
 struct EllView {
     int groups;
-    const int *off, *line, *idx;
+    const int *off, *line;
+    const unsigned short *idx;
     const float *vh, *vl;
 };
 
@@ -208,154 +211,267 @@ __device__ __forceinline__ float block_max(float v, float *red) {
     return m;
 }
 
-// The first pass for every chain flagged SEG_REPROJ (one CTA per chain at a
-// time), in double-float: d = S^T z (z the chain's GEMM row), dx = d, and
-// r = r0 - S d from the chain kernel's FP64 r0; r goes on in FP32 (Rf) and as
-// the next GEMM's BF16 split.
-template <bool EXACT32>
+// The first pass, in double-float, for CPB chains at a time per CTA (the
+// sparse structure each warp loads serves all of them): for every chain
+// flagged SEG_REPROJ, d = S^T z (z the chain's GEMM row), dx = d, and
+// r = r0 - S d from the chain kernel's FP64 r0; r goes on in FP32 (r) and as
+// the next GEMM's BF16 split.  Shared memory per chain: z (ldz floats), d as
+// hi and lo (2 ld floats).
+template <int CPB, bool EXACT32>
 __global__ void __launch_bounds__(kPassThreads) defer_pass1_kernel(const PassArgs a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ float red[kPassWarps];
-    float *zs = reinterpret_cast<float *>(smem_raw);
-    float *dh = zs + a.ldz;
-    float *dl = dh + a.ld;
+    __shared__ int live[CPB];
+    const size_t per = (size_t)a.ldz + 2 * (size_t)a.ld;
+    float *const sm = reinterpret_cast<float *>(smem_raw);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     if (*a.this_gate == 0ull) return;  // no chain's check fired (the GEMM did not run either)
     if (blockIdx.x == 0 && tid == 0) atomicAdd(a.counters + CNT_GEMMS, 1ull);
-    for (int p = blockIdx.x; p < a.P; p += gridDim.x) {
-        if (!(a.flags[p] & SEG_REPROJ)) continue;  // uniform over the block
-        const float *zp = a.Z + (size_t)p * (size_t)a.ldz;
-        for (int i = tid; i < a.m; i += kPassThreads) zs[i] = zp[i];
+    for (int p0 = blockIdx.x * CPB; p0 < a.P; p0 += gridDim.x * CPB) {
+        if (tid < CPB) live[tid] = (p0 + tid < a.P && (a.flags[p0 + tid] & SEG_REPROJ)) ? 1 : 0;
         __syncthreads();
-        float *dxh = a.dxh + (size_t)p * (size_t)a.ld, *dxl = a.dxl + (size_t)p * (size_t)a.ld;
+        int any = 0;
+#pragma unroll
+        for (int c = 0; c < CPB; ++c) any |= live[c];
+        if (!any) {
+            __syncthreads();
+            continue;
+        }
+#pragma unroll
+        for (int c = 0; c < CPB; ++c) {
+            if (!live[c]) continue;
+            const float *zp = a.Z + (size_t)(p0 + c) * (size_t)a.ldz;
+            float *zs = sm + c * per;
+            for (int i = tid; i < a.m; i += kPassThreads) zs[i] = zp[i];
+        }
+        __syncthreads();
         for (int g = warp; g < a.cols.groups; g += kPassWarps) {
             const int base = __ldg(a.cols.off + g);
             const int len = (__ldg(a.cols.off + g + 1) - base) >> 5;
-            float ah = 0.0f, al = 0.0f;
-#pragma unroll 4
+            float ah[CPB], al[CPB];
+#pragma unroll
+            for (int c = 0; c < CPB; ++c) ah[c] = al[c] = 0.0f;
+#pragma unroll 2
             for (int t = 0; t < len; ++t) {
                 const int q = base + (t << 5) + lane;
-                const float z = zs[__ldg(a.cols.idx + q)];
-                float ph, pe, s, e;
-                two_prod(__ldg(a.cols.vh + q), z, ph, pe);
-                if (!EXACT32) pe = fmaf(__ldg(a.cols.vl + q), z, pe);
-                two_sum(ah, ph, s, e);
-                ah = s;
-                al = __fadd_rn(al, __fadd_rn(e, pe));
+                const int i = __ldg(a.cols.idx + q);
+                const float sh = __ldg(a.cols.vh + q);
+                const float sl = EXACT32 ? 0.0f : __ldg(a.cols.vl + q);
+#pragma unroll
+                for (int c = 0; c < CPB; ++c) {
+                    const float z = sm[c * per + i];
+                    float ph, pe, s, e;
+                    two_prod(sh, z, ph, pe);
+                    if (!EXACT32) pe = fmaf(sl, z, pe);
+                    two_sum(ah[c], ph, s, e);
+                    ah[c] = s;
+                    al[c] = __fadd_rn(al[c], __fadd_rn(e, pe));
+                }
             }
-            float h, l;
-            fast_two_sum(ah, al, h, l);
             const int j = __ldg(a.cols.line + (g << 5) + lane);
             if (j >= 0) {
-                dh[j] = h;
-                dl[j] = l;
-                dxh[j] = h;
-                dxl[j] = l;
+#pragma unroll
+                for (int c = 0; c < CPB; ++c) {
+                    if (!live[c]) continue;
+                    float h, l;
+                    fast_two_sum(ah[c], al[c], h, l);
+                    float *dh = sm + c * per + a.ldz;
+                    dh[j] = h;
+                    dh[a.ld + j] = l;
+                    const size_t o = (size_t)(p0 + c) * (size_t)a.ld + (size_t)j;
+                    a.dxh[o] = h;
+                    a.dxl[o] = l;
+                }
             }
         }
         __syncthreads();
-        const double *rdp = a.rd + (size_t)p * (size_t)a.ldz;
-        float *rp = a.r + (size_t)p * (size_t)a.ldz;
-        __nv_bfloat16 *rh = a.Rh + (size_t)p * (size_t)a.kpad, *rl = a.Rl + (size_t)p * (size_t)a.kpad;
-        float mx = 0.0f, m0 = 0.0f;
+        float mx[CPB], m0[CPB];
+#pragma unroll
+        for (int c = 0; c < CPB; ++c) mx[c] = m0[c] = 0.0f;
         for (int g = warp; g < a.rows.groups; g += kPassWarps) {
             const int i = __ldg(a.rows.line + (g << 5) + lane);
-            float ah = 0.0f, al = 0.0f;
-            if (i >= 0) split_f64(rdp[i], ah, al);
-            m0 = fmaxf(m0, fabsf(ah));
+            float ah[CPB], al[CPB];
+#pragma unroll
+            for (int c = 0; c < CPB; ++c) {
+                ah[c] = al[c] = 0.0f;
+                if (i >= 0 && live[c]) split_f64(a.rd[(size_t)(p0 + c) * (size_t)a.ldz + (size_t)i], ah[c], al[c]);
+                m0[c] = fmaxf(m0[c], fabsf(ah[c]));
+            }
             const int base = __ldg(a.rows.off + g);
             const int len = (__ldg(a.rows.off + g + 1) - base) >> 5;
-#pragma unroll 4
+#pragma unroll 2
             for (int t = 0; t < len; ++t) {
                 const int q = base + (t << 5) + lane;
                 const int j = __ldg(a.rows.idx + q);
                 const float sh = __ldg(a.rows.vh + q);
-                const float xh = dh[j], xl = dl[j];
-                float ph, pe, s, e;
-                two_prod(sh, xh, ph, pe);
-                pe = fmaf(sh, xl, pe);
-                if (!EXACT32) pe = fmaf(__ldg(a.rows.vl + q), xh, pe);
-                two_sum(ah, -ph, s, e);
-                ah = s;
-                al = __fadd_rn(al, __fsub_rn(e, pe));
+                const float sl = EXACT32 ? 0.0f : __ldg(a.rows.vl + q);
+#pragma unroll
+                for (int c = 0; c < CPB; ++c) {
+                    const float *dh = sm + c * per + a.ldz;
+                    const float xh = dh[j], xl = dh[a.ld + j];
+                    float ph, pe, s, e;
+                    two_prod(sh, xh, ph, pe);
+                    pe = fmaf(sh, xl, pe);
+                    if (!EXACT32) pe = fmaf(sl, xh, pe);
+                    two_sum(ah[c], -ph, s, e);
+                    ah[c] = s;
+                    al[c] = __fadd_rn(al[c], __fsub_rn(e, pe));
+                }
             }
             if (i >= 0) {
-                const float rn = __fadd_rn(ah, al);
-                rp[i] = rn;
-                mx = fmaxf(mx, fabsf(rn));
-                if (!a.last) split_store(rn, rh, rl, i);
+#pragma unroll
+                for (int c = 0; c < CPB; ++c) {
+                    if (!live[c]) continue;
+                    const float rn = __fadd_rn(ah[c], al[c]);
+                    const size_t o = (size_t)(p0 + c) * (size_t)a.ldz + (size_t)i;
+                    a.r[o] = rn;
+                    mx[c] = fmaxf(mx[c], fabsf(rn));
+                    if (!a.last)
+                        split_store(rn, a.Rh + (size_t)(p0 + c) * (size_t)a.kpad,
+                                    a.Rl + (size_t)(p0 + c) * (size_t)a.kpad, i);
+                }
             }
         }
-        mx = block_max(mx, red);
-        m0 = block_max(m0, red);
-        if (tid == 0) {
-            a.flags[p] |= SEG_CORR;  // dx holds a correction for the next launch
-            a.r0[p] = m0;
-            pass_verdict(a, p, mx, m0);
+#pragma unroll
+        for (int c = 0; c < CPB; ++c) {
+            const float vmx = block_max(mx[c], red);
+            const float vm0 = block_max(m0[c], red);
+            if (tid == 0 && live[c]) {
+                const int p = p0 + c;
+                a.flags[p] |= SEG_CORR;  // dx holds a correction for the next launch
+                a.r0[p] = vm0;
+                pass_verdict(a, p, vmx, vm0);
+            }
         }
         __syncthreads();
     }
 }
 
-// A later pass (pass >= 1) for every chain still flagged SEG_REPROJ, in FP32:
-// d = S^T z, dx += d (double-float), r <- r - S d.
+// A later pass (pass >= 1), in FP32, for CPB chains at a time per CTA: for
+// every chain still flagged SEG_REPROJ, d = S^T z, dx += d (double-float),
+// r <- r - S d.  Shared memory per chain: z (ldz floats), d (ld floats).
+template <int CPB>
 __global__ void __launch_bounds__(kPassThreads) defer_pass_kernel(const PassArgs a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ float red[kPassWarps];
-    float *zs = reinterpret_cast<float *>(smem_raw);
-    float *ds = zs + a.ldz;
+    __shared__ int live[CPB];
+    const size_t per = (size_t)a.ldz + (size_t)a.ld;
+    float *const sm = reinterpret_cast<float *>(smem_raw);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     if (*a.this_gate == 0ull) return;  // no chain needed this pass (its GEMM did not run either)
     if (blockIdx.x == 0 && tid == 0) atomicAdd(a.counters + CNT_GEMMS, 1ull);
-    for (int p = blockIdx.x; p < a.P; p += gridDim.x) {
-        if (!(a.flags[p] & SEG_REPROJ)) continue;  // uniform over the block
-        const float *zp = a.Z + (size_t)p * (size_t)a.ldz;
-        for (int i = tid; i < a.m; i += kPassThreads) zs[i] = zp[i];
+    for (int p0 = blockIdx.x * CPB; p0 < a.P; p0 += gridDim.x * CPB) {
+        if (tid < CPB) live[tid] = (p0 + tid < a.P && (a.flags[p0 + tid] & SEG_REPROJ)) ? 1 : 0;
         __syncthreads();
-        float *dxh = a.dxh + (size_t)p * (size_t)a.ld, *dxl = a.dxl + (size_t)p * (size_t)a.ld;
+        int any = 0;
+#pragma unroll
+        for (int c = 0; c < CPB; ++c) any |= live[c];
+        if (!any) {
+            __syncthreads();
+            continue;
+        }
+#pragma unroll
+        for (int c = 0; c < CPB; ++c) {
+            if (!live[c]) continue;
+            const float *zp = a.Z + (size_t)(p0 + c) * (size_t)a.ldz;
+            float *zs = sm + c * per;
+            for (int i = tid; i < a.m; i += kPassThreads) zs[i] = zp[i];
+        }
+        __syncthreads();
         for (int g = warp; g < a.cols.groups; g += kPassWarps) {
             const int base = __ldg(a.cols.off + g);
             const int len = (__ldg(a.cols.off + g + 1) - base) >> 5;
-            float d = 0.0f;
+            float d[CPB];
+#pragma unroll
+            for (int c = 0; c < CPB; ++c) d[c] = 0.0f;
 #pragma unroll 4
             for (int t = 0; t < len; ++t) {
                 const int q = base + (t << 5) + lane;
-                d = fmaf(__ldg(a.cols.vh + q), zs[__ldg(a.cols.idx + q)], d);
+                const int i = __ldg(a.cols.idx + q);
+                const float sh = __ldg(a.cols.vh + q);
+#pragma unroll
+                for (int c = 0; c < CPB; ++c) d[c] = fmaf(sh, sm[c * per + i], d[c]);
             }
             const int j = __ldg(a.cols.line + (g << 5) + lane);
             if (j >= 0) {
-                ds[j] = d;
-                float s, e;
-                two_sum(dxh[j], d, s, e);
-                dxh[j] = s;
-                dxl[j] = __fadd_rn(dxl[j], e);
+#pragma unroll
+                for (int c = 0; c < CPB; ++c) {
+                    if (!live[c]) continue;
+                    sm[c * per + a.ldz + j] = d[c];
+                    const size_t o = (size_t)(p0 + c) * (size_t)a.ld + (size_t)j;
+                    float s, e;
+                    two_sum(a.dxh[o], d[c], s, e);
+                    a.dxh[o] = s;
+                    a.dxl[o] = __fadd_rn(a.dxl[o], e);
+                }
             }
         }
         __syncthreads();
-        float *rp = a.r + (size_t)p * (size_t)a.ldz;
-        __nv_bfloat16 *rh = a.Rh + (size_t)p * (size_t)a.kpad, *rl = a.Rl + (size_t)p * (size_t)a.kpad;
-        float mx = 0.0f;
+        float mx[CPB];
+#pragma unroll
+        for (int c = 0; c < CPB; ++c) mx[c] = 0.0f;
         for (int g = warp; g < a.rows.groups; g += kPassWarps) {
             const int base = __ldg(a.rows.off + g);
             const int len = (__ldg(a.rows.off + g + 1) - base) >> 5;
-            float acc = 0.0f;
+            float acc[CPB];
+#pragma unroll
+            for (int c = 0; c < CPB; ++c) acc[c] = 0.0f;
 #pragma unroll 4
             for (int t = 0; t < len; ++t) {
                 const int q = base + (t << 5) + lane;
-                acc = fmaf(__ldg(a.rows.vh + q), ds[__ldg(a.rows.idx + q)], acc);
+                const int j = __ldg(a.rows.idx + q);
+                const float sh = __ldg(a.rows.vh + q);
+#pragma unroll
+                for (int c = 0; c < CPB; ++c) acc[c] = fmaf(sh, sm[c * per + a.ldz + j], acc[c]);
             }
             const int i = __ldg(a.rows.line + (g << 5) + lane);
             if (i >= 0) {
-                const float rn = __fsub_rn(rp[i], acc);
-                rp[i] = rn;
-                mx = fmaxf(mx, fabsf(rn));
-                if (!a.last) split_store(rn, rh, rl, i);
+#pragma unroll
+                for (int c = 0; c < CPB; ++c) {
+                    if (!live[c]) continue;
+                    const size_t o = (size_t)(p0 + c) * (size_t)a.ldz + (size_t)i;
+                    const float rn = __fsub_rn(a.r[o], acc[c]);
+                    a.r[o] = rn;
+                    mx[c] = fmaxf(mx[c], fabsf(rn));
+                    if (!a.last)
+                        split_store(rn, a.Rh + (size_t)(p0 + c) * (size_t)a.kpad,
+                                    a.Rl + (size_t)(p0 + c) * (size_t)a.kpad, i);
+                }
             }
         }
-        mx = block_max(mx, red);
-        if (tid == 0) pass_verdict(a, p, mx, a.r0[p]);
+#pragma unroll
+        for (int c = 0; c < CPB; ++c) {
+            const float vmx = block_max(mx[c], red);
+            if (tid == 0 && live[c]) pass_verdict(a, p0 + c, vmx, a.r0[p0 + c]);
+        }
         __syncthreads();
     }
+}
+
+// The pass kernels and their shared memory for a model: the most chains per
+// CTA (4, 2 or 1) whose shared memory fits.
+struct PassPlan {
+    void (*pass1)(PassArgs);
+    void (*pass)(PassArgs);
+    size_t smem1, smem;
+    int cpb1, cpb;
+};
+
+PassPlan plan_passes(long long ld, long long ldz, bool exact32) {
+    PassPlan pl{};
+    const size_t per1 = sizeof(float) * ((size_t)ldz + 2 * (size_t)ld), per = sizeof(float) * ((size_t)ldz + (size_t)ld);
+    pl.cpb1 = per1 * 4 <= kPassSmemMax ? 4 : per1 * 2 <= kPassSmemMax ? 2 : 1;
+    pl.cpb = per * 4 <= kPassSmemMax ? 4 : per * 2 <= kPassSmemMax ? 2 : 1;
+    pl.smem1 = per1 * (size_t)pl.cpb1;
+    pl.smem = per * (size_t)pl.cpb;
+    if (exact32)
+        pl.pass1 = pl.cpb1 == 4 ? defer_pass1_kernel<4, true> : pl.cpb1 == 2 ? defer_pass1_kernel<2, true>
+                                                                              : defer_pass1_kernel<1, true>;
+    else
+        pl.pass1 = pl.cpb1 == 4 ? defer_pass1_kernel<4, false> : pl.cpb1 == 2 ? defer_pass1_kernel<2, false>
+                                                                               : defer_pass1_kernel<1, false>;
+    pl.pass = pl.cpb == 4 ? defer_pass_kernel<4> : pl.cpb == 2 ? defer_pass_kernel<2> : defer_pass_kernel<1>;
+    return pl;
 }
 
 // Sliced-ELL block of the lines of a sparse matrix given as CSR-like
@@ -368,7 +484,8 @@ achr_status build_ell(SlicedEll &E, int n_lines, const std::vector<int> &ptr, co
         return ptr[(size_t)a + 1] - ptr[(size_t)a] > ptr[(size_t)b + 1] - ptr[(size_t)b];
     });
     const int groups = (n_lines + 31) / 32;
-    std::vector<int> off((size_t)groups + 1, 0), line((size_t)groups * 32, -1), eidx;
+    std::vector<int> off((size_t)groups + 1, 0), line((size_t)groups * 32, -1);
+    std::vector<unsigned short> eidx;
     std::vector<float> vh, vl;
     for (int g = 0; g < groups; ++g) {
         int len = 0;
@@ -386,7 +503,7 @@ achr_status build_ell(SlicedEll &E, int n_lines, const std::vector<int> &ptr, co
                 const float h = (float)v;
                 const float lo = (float)(v - (double)h);
                 if (lo != 0.0f) exact32 = false;
-                eidx.push_back(real ? idx[(size_t)ptr[(size_t)L] + t] : 0);
+                eidx.push_back((unsigned short)(real ? idx[(size_t)ptr[(size_t)L] + t] : 0));
                 vh.push_back(h);
                 vl.push_back(lo);
             }
@@ -513,13 +630,13 @@ achr_status defer_sample(achr_ctx *ctx, const ChainArgs &a_in, int threads_per_c
     int dev = 0, sms = 0, per_sm = 0, per_sm1 = 0;
     DEFER_TRY(cudaGetDevice(&dev));
     DEFER_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    const size_t pass_smem = sizeof(float) * ((size_t)D.ldz + (size_t)D.ld);
-    const size_t pass1_smem = sizeof(float) * ((size_t)D.ldz + 2 * (size_t)D.ld);
-    auto *const pass1 = D.exact32 ? defer_pass1_kernel<true> : defer_pass1_kernel<false>;
-    DEFER_TRY(cudaFuncSetAttribute(defer_pass_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pass_smem));
-    DEFER_TRY(cudaFuncSetAttribute(pass1, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pass1_smem));
-    DEFER_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, defer_pass_kernel, kPassThreads, pass_smem));
-    DEFER_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm1, pass1, kPassThreads, pass1_smem));
+    const PassPlan pl = plan_passes(D.ld, D.ldz, D.exact32);
+    if (pl.smem1 > kPassSmemMax || pl.smem > kPassSmemMax)
+        return set_err(ACHR_ERR_UNSUPPORTED, "model too large for the batched reprojection's shared memory");
+    DEFER_TRY(cudaFuncSetAttribute(pl.pass, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pl.smem));
+    DEFER_TRY(cudaFuncSetAttribute(pl.pass1, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pl.smem1));
+    DEFER_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pl.pass, kPassThreads, pl.smem));
+    DEFER_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm1, pl.pass1, kPassThreads, pl.smem1));
     if (per_sm < 1 || per_sm1 < 1)
         return set_err(ACHR_ERR_UNSUPPORTED, "model too large for the batched reprojection's update");
 
@@ -550,8 +667,8 @@ achr_status defer_sample(achr_ctx *ctx, const ChainArgs &a_in, int threads_per_c
         a.ld_r = D.ldz;
         a.seg_dxh = D.dxh.p;
         a.seg_dxl = D.dxl.p;
-        const int pass_grid = (int)std::min<long long>((long long)sms * per_sm, pc);
-        const int pass1_grid = (int)std::min<long long>((long long)sms * per_sm1, pc);
+        const int pass_grid = (int)std::min<long long>((long long)sms * per_sm, (pc + pl.cpb - 1) / pl.cpb);
+        const int pass1_grid = (int)std::min<long long>((long long)sms * per_sm1, (pc + pl.cpb1 - 1) / pl.cpb1);
         PassArgs pa{};
         pa.n = ctx->n;
         pa.m = ctx->m;
@@ -602,8 +719,8 @@ achr_status defer_sample(achr_ctx *ctx, const ChainArgs &a_in, int threads_per_c
                 pa.last = pass + 1 == passes ? 1 : 0;
                 pa.this_gate = gate + pass;
                 pa.next_any = gate + pass + 1;
-                if (pass == 0) pass1<<<(unsigned)pass1_grid, kPassThreads, pass1_smem, s>>>(pa);
-                else defer_pass_kernel<<<(unsigned)pass_grid, kPassThreads, pass_smem, s>>>(pa);
+                if (pass == 0) pl.pass1<<<(unsigned)pass1_grid, kPassThreads, pl.smem1, s>>>(pa);
+                else pl.pass<<<(unsigned)pass_grid, kPassThreads, pl.smem, s>>>(pa);
                 DEFER_TRY(cudaGetLastError());
                 ctx->last_launches += 2;
             }

@@ -96,8 +96,8 @@ typedef struct {
                                     and the dense product on the tensor cores (three BF16 split
                                     products); the first pass's update S^T z and new residual are
                                     exact to double-float (~48 bits), later ones (FP32, on what is left)
-                                    run per chain until max|S x| <= max(residual_tol / 1000, 1e-9 of the
-                                    residual the check found); then the clip and the centre update of
+                                    run per chain until max|S x| <= residual_tol / 1000; then the clip
+                                    and the centre update of
                                     that step, as the reference orders them; needs n_mets <= the chain
                                     kernel's padded length and a condition number of S S^T <= 2e4
                                     (achr_sample,
