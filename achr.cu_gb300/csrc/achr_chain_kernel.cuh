@@ -1022,10 +1022,9 @@ __global__ void __launch_bounds__(BD, (BD <= 384 ? 2 : 1)) achr_chain_kernel(con
                             // integer operations, and the FP64 value is stored as it is)
                             unsigned short h, l;
                             split_bf16_bits(f64_to_f32_rz(rr[q]), h, l);
-                            const int row = __ldg(a.row_orig + q);
-                            rh[row] = h;
-                            rl[row] = l;
-                            rd[row] = rr[q];
+                            rh[q] = h;  // device row order, as the batched passes read them
+                            rl[q] = l;
+                            rd[q] = rr[q];
                         }
                     }
 #pragma unroll

@@ -40,7 +40,11 @@
 // (which chains reproject) are the chain kernel's own FP64 residual, identical
 // to the check it makes when it reprojects in place.  S and S^T are read as
 // sliced-ELL blocks (32 lines per group, slot-major, lines sorted by length)
-// so a warp's loads of one slot are one coalesced segment.
+// so a warp's loads of one slot are one coalesced segment.  Every per-row
+// quantity (S x, R, Z = R B^T, r) is kept in the chain kernel's device row
+// order (rows longest first), with B permuted to match, so the chain kernel
+// and the passes read and write them as contiguous runs; the per-reaction
+// update leaves the passes through shared memory in reaction order.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -81,8 +85,8 @@ struct DeferState {
     DevBuf<float> r;         // cap x ldz: r after each pass, FP32
     DevBuf<float> dxh, dxl;  // cap x ld: the passes' summed correction S^T z, double-float
     DevBuf<float> r0;        // cap: max|S x| of the chain when its check fired
-    SlicedEll cols, rows;    // S^T and S, model row order
-    DevBuf<int> row_orig;    // m: device row order of S -> the model's row order
+    SlicedEll cols, rows;    // S^T and S; rows of S (and the row indices of S^T) in the device row order
+    DevBuf<__nv_bfloat16> Bh, Bl;  // m x kpad: (S S^T)^+ split into hi + lo, rows and columns in the device row order
     DevBuf<unsigned long long> any;  // one word per launch and pass: some chain needs that pass
     int any_cap = 0;
     // Timing of the last run (only when requested): an event before and after every
@@ -278,13 +282,21 @@ __global__ void __launch_bounds__(kPassThreads) defer_pass1_kernel(const PassArg
                     float *dh = sm + c * per + a.ldz;
                     dh[j] = h;
                     dh[a.ld + j] = l;
-                    const size_t o = (size_t)(p0 + c) * (size_t)a.ld + (size_t)j;
-                    a.dxh[o] = h;
-                    a.dxl[o] = l;
                 }
             }
         }
         __syncthreads();
+        // d leaves shared memory in reaction order (the lines above run in column-length order)
+#pragma unroll
+        for (int c = 0; c < CPB; ++c) {
+            if (!live[c]) continue;
+            const float *dh = sm + c * per + a.ldz;
+            float *gh = a.dxh + (size_t)(p0 + c) * (size_t)a.ld, *gl = a.dxl + (size_t)(p0 + c) * (size_t)a.ld;
+            for (int j = tid; j < a.n; j += kPassThreads) {
+                gh[j] = dh[j];
+                gl[j] = dh[a.ld + j];
+            }
+        }
         float mx[CPB], m0[CPB];
 #pragma unroll
         for (int c = 0; c < CPB; ++c) mx[c] = m0[c] = 0.0f;
@@ -395,18 +407,24 @@ __global__ void __launch_bounds__(kPassThreads) defer_pass_kernel(const PassArgs
             const int j = __ldg(a.cols.line + (g << 5) + lane);
             if (j >= 0) {
 #pragma unroll
-                for (int c = 0; c < CPB; ++c) {
-                    if (!live[c]) continue;
-                    sm[c * per + a.ldz + j] = d[c];
-                    const size_t o = (size_t)(p0 + c) * (size_t)a.ld + (size_t)j;
-                    float s, e;
-                    two_sum(a.dxh[o], d[c], s, e);
-                    a.dxh[o] = s;
-                    a.dxl[o] = __fadd_rn(a.dxl[o], e);
-                }
+                for (int c = 0; c < CPB; ++c)
+                    if (live[c]) sm[c * per + a.ldz + j] = d[c];
             }
         }
         __syncthreads();
+        // dx += d in reaction order (the lines above run in column-length order)
+#pragma unroll
+        for (int c = 0; c < CPB; ++c) {
+            if (!live[c]) continue;
+            const float *ds = sm + c * per + a.ldz;
+            float *gh = a.dxh + (size_t)(p0 + c) * (size_t)a.ld, *gl = a.dxl + (size_t)(p0 + c) * (size_t)a.ld;
+            for (int j = tid; j < a.n; j += kPassThreads) {
+                float s, e;
+                two_sum(gh[j], ds[j], s, e);
+                gh[j] = s;
+                gl[j] = __fadd_rn(gl[j], e);
+            }
+        }
         float mx[CPB];
 #pragma unroll
         for (int c = 0; c < CPB; ++c) mx[c] = 0.0f;
@@ -475,14 +493,16 @@ PassPlan plan_passes(long long ld, long long ldz, bool exact32) {
 }
 
 // Sliced-ELL block of the lines of a sparse matrix given as CSR-like
-// (ptr, idx, val) over n_lines lines; lines sorted by length, longest first.
+// (ptr, idx, val) over n_lines lines; with `sort`, lines sorted by length,
+// longest first, else line l of the block is line l of the matrix.
 achr_status build_ell(SlicedEll &E, int n_lines, const std::vector<int> &ptr, const std::vector<int> &idx,
-                      const std::vector<double> &val, bool &exact32) {
+                      const std::vector<double> &val, bool &exact32, bool sort) {
     std::vector<int> order((size_t)n_lines);
     for (int l = 0; l < n_lines; ++l) order[(size_t)l] = l;
-    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
-        return ptr[(size_t)a + 1] - ptr[(size_t)a] > ptr[(size_t)b + 1] - ptr[(size_t)b];
-    });
+    if (sort)
+        std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+            return ptr[(size_t)a + 1] - ptr[(size_t)a] > ptr[(size_t)b + 1] - ptr[(size_t)b];
+        });
     const int groups = (n_lines + 31) / 32;
     std::vector<int> off((size_t)groups + 1, 0), line((size_t)groups * 32, -1);
     std::vector<unsigned short> eidx;
@@ -517,6 +537,25 @@ achr_status build_ell(SlicedEll &E, int n_lines, const std::vector<int> &ptr, co
     return ACHR_OK;
 }
 
+// B in the device row order: Bd[q][q'] = B[order[q]][order[q']] (q' < m; the K padding stays
+// zero), so that the chain kernel's residual rows, R, Z and r all use the row order in which the
+// chain kernel computes S x and every access to them is coalesced.
+__global__ void permute_pinv(int m, int kpad, const int *__restrict__ order, const __nv_bfloat16 *__restrict__ Bh,
+                             const __nv_bfloat16 *__restrict__ Bl, __nv_bfloat16 *__restrict__ Dh,
+                             __nv_bfloat16 *__restrict__ Dl) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)m * kpad) return;
+    const int q = (int)(t / kpad), k = (int)(t % kpad);
+    if (k >= m) {
+        Dh[t] = __float2bfloat16_rn(0.0f);
+        Dl[t] = __float2bfloat16_rn(0.0f);
+        return;
+    }
+    const size_t src = (size_t)__ldg(order + q) * (size_t)kpad + (size_t)__ldg(order + k);
+    Dh[t] = Bh[src];
+    Dl[t] = Bl[src];
+}
+
 EllView view(const SlicedEll &E) {
     return EllView{E.groups, E.off.p, E.line.p, E.idx.p, E.vh.p, E.vl.p};
 }
@@ -531,11 +570,32 @@ achr_status ensure_defer(achr_ctx *ctx, int chains, int segments) {
         D->kpad = R.kpad;
         D->ld = (ctx->n + 1) & ~1;
         D->ldz = (ctx->m + 3) & ~3;
-        DEFER_TRY(D->row_orig.upload(ctx->h_row_order.data(), ctx->h_row_order.size()));
-        // S (rows) and S^T (columns of S) in the model's row order, the order of B's rows.
         const int n = ctx->n, m = ctx->m;
-        const std::vector<int> &rp = ctx->h_rowptr, &ci = ctx->h_colidx;
-        const std::vector<double> &rv = ctx->h_val;
+        const std::vector<int> &order = ctx->h_row_order;  // device row q = model row order[q]
+        {
+            DevBuf<int> ord;
+            DEFER_TRY(ord.upload(order.data(), order.size()));
+            const size_t cnt = (size_t)m * (size_t)D->kpad;
+            DEFER_TRY(D->Bh.alloc(cnt));
+            DEFER_TRY(D->Bl.alloc(cnt));
+            permute_pinv<<<(unsigned)((cnt + 255) / 256), 256>>>(m, D->kpad, ord.p, R.Bh.p, R.Bl.p, D->Bh.p, D->Bl.p);
+            DEFER_TRY(cudaGetLastError());
+            DEFER_TRY(cudaDeviceSynchronize());
+        }
+        // S (rows) and S^T (columns of S), rows in the device order: longest first, the order
+        // the chain kernel computes S x in, so the rows block keeps that order.
+        std::vector<int> rp((size_t)m + 1, 0), ci;
+        std::vector<double> rv;
+        ci.reserve(ctx->h_colidx.size());
+        rv.reserve(ctx->h_val.size());
+        for (int q = 0; q < m; ++q) {
+            const int r = order[(size_t)q];
+            for (int t = ctx->h_rowptr[(size_t)r]; t < ctx->h_rowptr[(size_t)r + 1]; ++t) {
+                ci.push_back(ctx->h_colidx[(size_t)t]);
+                rv.push_back(ctx->h_val[(size_t)t]);
+            }
+            rp[(size_t)q + 1] = (int)ci.size();
+        }
         std::vector<int> cp((size_t)n + 1, 0), ri(ci.size());
         std::vector<double> cv(ci.size());
         for (int c : ci) cp[(size_t)c + 1]++;
@@ -550,9 +610,9 @@ achr_status ensure_defer(achr_ctx *ctx, int chains, int segments) {
                 }
         }
         bool exact = true;
-        achr_status st = build_ell(D->cols, n, cp, ri, cv, exact);
+        achr_status st = build_ell(D->cols, n, cp, ri, cv, exact, true);
         if (st != ACHR_OK) return st;
-        st = build_ell(D->rows, m, rp, ci, rv, exact);
+        st = build_ell(D->rows, m, rp, ci, rv, exact, false);  // line q is device row q
         if (st != ACHR_OK) return st;
         D->exact32 = exact;
     }
@@ -659,7 +719,6 @@ achr_status defer_sample(achr_ctx *ctx, const ChainArgs &a_in, int threads_per_c
         a.seg_A = D.A.p;
         a.ld_seg = D.ld;
         a.seg_flags = D.flags.p;
-        a.row_orig = D.row_orig.p;
         a.seg_Rh = D.Rh.p;
         a.seg_Rl = D.Rl.p;
         a.kpad = D.kpad;
@@ -709,7 +768,7 @@ achr_status defer_sample(achr_ctx *ctx, const ChainArgs &a_in, int threads_per_c
             ++ctx->last_launches;
             if (!ends_on_check) break;
             for (int pass = 0; pass < passes; ++pass) {
-                TcGemm g{pc, R.m, R.kpad, 3, D.Rh.p, D.Rl.p, (long long)R.kpad, R.Bh.p, R.Bl.p, (long long)R.kpad,
+                TcGemm g{pc, R.m, R.kpad, 3, D.Rh.p, D.Rl.p, (long long)R.kpad, D.Bh.p, D.Bl.p, (long long)R.kpad,
                          D.Z.p, (long long)D.ldz};
                 g.gate = gate + pass;  // skipped when no chain needs this pass
                 g.gate_max = 0;

@@ -96,10 +96,9 @@ struct ChainArgs {
     long long ld_seg;
     unsigned *seg_flags;           // per chain, SEG_* bits
     unsigned long long *seg_any;   // set to 1 when a chain of this launch needs a reprojection
-    const int *row_orig;           // device row q of S -> row in the model's order
-    unsigned short *seg_Rh, *seg_Rl;  // P x kpad BF16 bits: hi and lo parts of S x
+    unsigned short *seg_Rh, *seg_Rl;  // P x kpad BF16 bits: hi and lo parts of S x (device row order)
     int kpad;
-    double *seg_rd;                // P x ld_r: S x at the check (FP64), rows in the model's order
+    double *seg_rd;                // P x ld_r: S x at the check (FP64), device row order
     long long ld_r;
     const float *seg_dxh, *seg_dxl;  // P x ld_seg: the passes' correction (double-float), subtracted next launch
 };

@@ -47,3 +47,20 @@ def reference_form_case(pkg, spec, n_warmup, tmp_dir, seed=17):
 def rel_err(a, b):
     """Largest difference relative to max(1, max|b|), the parity tests' measure."""
     return float(np.abs(a - b).max() / max(1.0, np.abs(b).max()))
+
+
+def refined_null_space(S, N):
+    """N with its component in the row space of S removed, re-orthonormalised.
+
+    A null-space basis from an FP64 factorisation is orthogonal to the rows of S
+    only to a few 1e-15 (the small fixture's: 4.6e-15).  The deferred
+    reprojection removes the row-space part of x itself, x - S^T (S S^T)^+ S x,
+    while the oracle applies N (N^T x), so that residue separates the two, and
+    a later hit-and-run step bounded by a tiny direction component can
+    multiply it a thousandfold.  One application of the projector and a QR
+    (signs fixed so the columns keep their direction) bring it to 6e-16.
+    """
+    S = np.asarray(S, dtype=np.float64)
+    N1 = N - S.T @ (np.linalg.pinv(S @ S.T) @ (S @ N))
+    Q, R = np.linalg.qr(N1)
+    return np.ascontiguousarray(Q * np.sign(np.diag(R))[None, :])

@@ -15,7 +15,7 @@ from __future__ import annotations
 import numpy as np
 import pytest
 
-from cases import rel_err
+from cases import refined_null_space, rel_err
 from conftest import dense_S
 
 pytestmark = pytest.mark.gpu
@@ -45,10 +45,14 @@ def test_deferred_matches_oracle(deferred, oracle_mod, small_model, golden, step
 
 @pytest.mark.parametrize("period,steps", [(1, 12), (7, 30), (25, 60)])
 def test_deferred_other_check_periods(pkg, oracle_mod, small_model, golden, period, steps):
+    """With 25 steps between checks the points drift far enough from the null space that the
+    oracle's N (N^T x) shows the basis's own 1e-15 row-space residue, and one chain's later
+    steps amplify it past the bar: both sides use a basis refined to rounding level."""
+    N = refined_null_space(dense_S(small_model), golden["N"])
     with pkg.Sampler(small_model, golden["warmup"], reproject_form=3, check_period=period) as s:
-        s.set_null_space(golden["N"])
+        s.set_null_space(N)
         pts, st = s.sample(32, steps, seed=5)
-    ref, rst = oracle_mod.sample(small_model, golden["warmup"], golden["N"], 5, 32, steps, check_period=period)
+    ref, rst = oracle_mod.sample(small_model, golden["warmup"], N, 5, 32, steps, check_period=period)
     assert st["checks"] == rst["checks"] and st["reprojections"] == rst["reprojections"] > 0
     assert rel_err(pts, ref) <= REL_TOL
 
