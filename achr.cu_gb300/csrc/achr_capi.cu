@@ -966,28 +966,116 @@ achr_status achr_sample_batch(achr_ctx *const *ctxs, int32_t n_models, const int
     int dev = 0, sms = 0;
     ACHR_CUDA_TRY(cudaGetDevice(&dev));
     ACHR_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    // Predicted time of each model orders the launches.
-    std::vector<double> work((size_t)n_models);
-    std::vector<int> per_sm((size_t)n_models);
-    std::vector<uint64_t> offset((size_t)n_models);
-    double total = 0.0;
+    // Per model: its configuration, its launch arguments and the predicted time of one chain.
+    std::vector<ChainArgs> args((size_t)n_models);
+    std::vector<double> chain_time((size_t)n_models);
+    std::vector<int> cfg_key((size_t)n_models);
     uint64_t off = 0;
     for (int k = 0; k < n_models; ++k) {
         achr_ctx *c = ctxs[k];
         if (!c || n_points[k] < 0 || (n_points[k] > 0 && (!d_points_out[k] || ld_out[k] < n_points[k])))
             return fail(ACHR_ERR_INVALID, "bad batch entry " + std::to_string(k));
-        const ChainArgs a0 = chain_args(c, seed, 0, 0, n_steps, d_points_out[k], ld_out[k]);
-        cudaError_t e = achr::launch_chains(a0, c->opt.threads_per_chain, nullptr, 0, &per_sm[(size_t)k]);
-        if (e != cudaSuccess) return cuda_fail(e, "chain kernel configuration");
-        // predicted time on the whole GPU: measured by the autotuner, else padded elements x chain-steps
-        work[(size_t)k] = c->tuned_rate > 0
-                              ? (double)n_points[k] * (double)n_steps / c->tuned_rate
-                              : (double)n_points[k] * (double)n_steps *
-                                    (double)achr::chain_padded_length(c->n, c->opt.threads_per_chain) * 1e-9;
-        total += work[(size_t)k];
-        offset[(size_t)k] = off;  // disjoint chain ids: model k uses ids off .. off + P_k - 1
+        int bd = 0, ept = 0;
+        if (!achr::chain_config(c->n, c->opt.threads_per_chain, &bd, &ept) || bd * ept > c->np)
+            return fail(ACHR_ERR_UNSUPPORTED, "no chain-kernel configuration for batch entry " + std::to_string(k));
+        cfg_key[(size_t)k] = bd * 100 + ept;
+        // disjoint chain ids: model k uses ids off .. off + P_k - 1
+        args[(size_t)k] = chain_args(c, seed, off, n_points[k], n_steps, d_points_out[k], ld_out[k]);
         off += (uint64_t)n_points[k];
+        // measured by the autotuner (whole-GPU rate), else padded elements x steps
+        chain_time[(size_t)k] = c->tuned_rate > 0 ? (double)n_steps / c->tuned_rate
+                                                  : (double)n_steps * (double)(bd * ept) * 1e-9;
     }
+    // One work queue per configuration.  Items run longest model first; each
+    // item's tile of chains is sized (guided self-scheduling) to about a
+    // quarter of the work still queued behind it divided by the CTAs, so
+    // early items are large (few queue operations) and the last ones are
+    // single chains (the launch ends evenly).
+    struct Group {
+        int bd, ept, grid = 0;
+        std::vector<int> models;
+        std::vector<int4> items;
+        double work = 0.0;
+        size_t extra = 0;
+    };
+    std::vector<Group> groups;
+    for (int k = 0; k < n_models; ++k) {
+        size_t g = 0;
+        while (g < groups.size() && groups[g].bd * 100 + groups[g].ept != cfg_key[(size_t)k]) ++g;
+        if (g == groups.size()) {
+            Group ng;
+            ng.bd = cfg_key[(size_t)k] / 100;
+            ng.ept = cfg_key[(size_t)k] % 100;
+            groups.push_back(ng);
+        }
+        groups[g].models.push_back(k);
+        groups[g].work += (double)n_points[k] * chain_time[(size_t)k];
+    }
+    size_t total_items = 0;
+    for (Group &G : groups) {
+        // The residual-form reprojection keeps (S S^T)^+ r in shared memory: the
+        // group keeps it only if that costs no resident CTA per SM.
+        size_t extra = 0;
+        for (int k : G.models) {
+            ChainArgs &a = args[(size_t)k];
+            if (a.pinv32 && a.m > G.bd * G.ept) a.pinv32 = nullptr;
+            if (a.pinv32) extra = std::max(extra, ((size_t)a.m * sizeof(float) + 15) & ~(size_t)15);
+        }
+        achr::ChainQueue probe{};
+        int per_sm = 0, per_sm_z = 0;
+        cudaError_t e = achr::launch_chain_queue(G.bd, G.ept, probe, nullptr, 0, &per_sm);
+        if (e != cudaSuccess) return cuda_fail(e, "work-queue kernel configuration");
+        if (extra) {
+            probe.extra_smem = extra;
+            e = achr::launch_chain_queue(G.bd, G.ept, probe, nullptr, 0, &per_sm_z);
+            if (e != cudaSuccess || per_sm_z < per_sm) {
+                (void)cudaGetLastError();
+                extra = 0;
+                for (int k : G.models) args[(size_t)k].pinv32 = nullptr;
+            }
+        }
+        G.extra = extra;
+        G.grid = sms * per_sm;
+        std::stable_sort(G.models.begin(), G.models.end(),
+                         [&](int x, int y) { return chain_time[(size_t)x] > chain_time[(size_t)y]; });
+        double left = G.work;
+        for (int k : G.models) {
+            const double t = chain_time[(size_t)k];
+            for (int p = 0; p < n_points[k];) {
+                long long tile = (long long)(left / (4.0 * G.grid * std::max(t, 1e-30)));
+                tile = std::max(1LL, std::min(tile, (long long)(n_points[k] - p)));
+                G.items.push_back(make_int4(k, p, p + (int)tile, 0));
+                p += (int)tile;
+                left -= (double)tile * t;
+            }
+        }
+        total_items += G.items.size();
+    }
+    std::stable_sort(groups.begin(), groups.end(), [](const Group &x, const Group &y) { return x.work > y.work; });
+
+    // Device copies: the models' arguments, the items of every group, and the
+    // queue heads, per-model done counts and finish stamps (zeroed in the graph).
+    DevBuf<ChainArgs> d_args;
+    DevBuf<int4> d_items;
+    DevBuf<int> d_ints;  // [0, groups): queue heads, [groups, groups + n_models): chains done
+    DevBuf<unsigned long long> stamps;
+    ACHR_CUDA_TRY(d_args.upload(args.data(), args.size()));
+    {
+        std::vector<int4> all;
+        all.reserve(total_items);
+        for (const Group &G : groups) all.insert(all.end(), G.items.begin(), G.items.end());
+        ACHR_CUDA_TRY(d_items.upload(all.data(), all.size()));
+    }
+    const size_t n_ints = groups.size() + (size_t)n_models;
+    ACHR_CUDA_TRY(d_ints.alloc(n_ints));
+    size_t n_ctas = 0;
+    for (Group &G : groups) {
+        G.grid = (int)std::min<size_t>((size_t)G.grid, G.items.size());
+        n_ctas += (size_t)G.grid;
+    }
+    // [0, n_models): each model's finish, [n_models]: graph start, then one per CTA: its exit
+    ACHR_CUDA_TRY(stamps.alloc((size_t)n_models + 1 + n_ctas));
+
     cudaStream_t main = (cudaStream_t)stream;
     StreamSet ss;
     if (main == nullptr) {  // the legacy default stream cannot be captured: use a private stream
@@ -997,42 +1085,45 @@ achr_status achr_sample_batch(achr_ctx *const *ctxs, int32_t n_models, const int
         main = own;
     }
     const size_t first = ss.streams.size();
-    ss.streams.resize(first + (size_t)n_models, nullptr);
-    ss.events.resize((size_t)n_models + 3, nullptr);
+    ss.streams.resize(first + groups.size(), nullptr);
+    ss.events.resize(groups.size() + 3, nullptr);
     for (size_t q = first; q < ss.streams.size(); ++q)
         ACHR_CUDA_TRY(cudaStreamCreateWithFlags(&ss.streams[q], cudaStreamNonBlocking));
     for (auto &ev : ss.events) ACHR_CUDA_TRY(cudaEventCreate(&ev));
-    cudaEvent_t fork = ss.events[(size_t)n_models], t0 = ss.events[(size_t)n_models + 1],
-                t1 = ss.events[(size_t)n_models + 2];
-    DevBuf<unsigned long long> stamps;  // [0, n_models): each model's finish, [n_models]: graph start
-    ACHR_CUDA_TRY(stamps.alloc((size_t)n_models + 1));
-    // One graph: fork, one persistent chain kernel per model on its own stream
-    // (grid = its share of the SMs x resident CTAs), join.
+    const size_t ng = groups.size();
+    cudaEvent_t fork = ss.events[ng], t0 = ss.events[ng + 1], t1 = ss.events[ng + 2];
+    // One graph: zero the queue state and every model's counters, fork, one
+    // persistent work-queue kernel per configuration (largest total work
+    // first) on its own stream, join.
     cudaGraph_t graph = nullptr;
     ACHR_CUDA_TRY(cudaStreamBeginCapture(main, cudaStreamCaptureModeThreadLocal));
-    stamp_kernel<<<1, 1, 0, main>>>(stamps.p + n_models);
-    cudaError_t ce = cudaGetLastError();
+    cudaError_t ce = cudaMemsetAsync(d_ints.p, 0, sizeof(int) * n_ints, main);
+    for (int k = 0; k < n_models && ce == cudaSuccess; ++k)
+        ce = cudaMemsetAsync(ctxs[k]->counters.p, 0, sizeof(unsigned long long) * achr::CNT_SLOTS, main);
+    if (ce == cudaSuccess) {
+        stamp_kernel<<<1, 1, 0, main>>>(stamps.p + n_models);
+        ce = cudaGetLastError();
+    }
     if (ce == cudaSuccess) ce = cudaEventRecord(fork, main);
-    // Longest predicted model first; one CTA per chain, so the CTA scheduler
-    // hands every SM slot that frees up to whichever model still has chains.
-    std::vector<int> order((size_t)n_models);
-    for (int k = 0; k < n_models; ++k) order[(size_t)k] = k;
-    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return work[(size_t)x] > work[(size_t)y]; });
-    for (int q = 0; q < n_models && ce == cudaSuccess; ++q) {
-        const int k = order[(size_t)q];
-        cudaStream_t sk = ss.streams[first + (size_t)k];
-        achr_ctx *c = ctxs[k];
-        ce = cudaStreamWaitEvent(sk, fork, 0);
-        if (ce == cudaSuccess)
-            ce = cudaMemsetAsync(c->counters.p, 0, sizeof(unsigned long long) * achr::CNT_SLOTS, sk);
-        const ChainArgs a = chain_args(c, seed, offset[(size_t)k], n_points[k], n_steps, d_points_out[k], ld_out[k]);
-        if (ce == cudaSuccess) ce = achr::launch_chains(a, c->opt.threads_per_chain, sk, -1);
-        if (ce == cudaSuccess) {
-            stamp_kernel<<<1, 1, 0, sk>>>(stamps.p + k);
-            ce = cudaGetLastError();
-        }
-        if (ce == cudaSuccess) ce = cudaEventRecord(ss.events[(size_t)k], sk);
-        if (ce == cudaSuccess) ce = cudaStreamWaitEvent(main, ss.events[(size_t)k], 0);
+    size_t item0 = 0, cta0 = (size_t)n_models + 1;
+    for (size_t g = 0; g < ng && ce == cudaSuccess; ++g) {
+        const Group &G = groups[g];
+        cudaStream_t sg = ss.streams[first + g];
+        achr::ChainQueue q{};
+        q.args = d_args.p;
+        q.items = d_items.p + item0;
+        q.n_items = (int)G.items.size();
+        q.next = d_ints.p + g;
+        q.chains_done = d_ints.p + ng;
+        q.done_ns = stamps.p;
+        q.extra_smem = G.extra;
+        q.cta_ns = stamps.p + cta0;
+        item0 += G.items.size();
+        cta0 += (size_t)G.grid;
+        ce = cudaStreamWaitEvent(sg, fork, 0);
+        if (ce == cudaSuccess) ce = achr::launch_chain_queue(G.bd, G.ept, q, sg, G.grid, nullptr);
+        if (ce == cudaSuccess) ce = cudaEventRecord(ss.events[g], sg);
+        if (ce == cudaSuccess) ce = cudaStreamWaitEvent(main, ss.events[g], 0);
     }
     cudaError_t ee = cudaStreamEndCapture(main, &graph);
     if (ce != cudaSuccess || ee != cudaSuccess) {
@@ -1051,15 +1142,12 @@ achr_status achr_sample_batch(achr_ctx *const *ctxs, int32_t n_models, const int
     if (ce != cudaSuccess) return cuda_fail(ce, "batched graph launch");
     float total_ms = 0.0f;
     ACHR_CUDA_TRY(cudaEventElapsedTime(&total_ms, t0, t1));
-    std::vector<unsigned long long> ts((size_t)n_models + 1);
+    std::vector<unsigned long long> ts((size_t)n_models + 1 + n_ctas);
     ACHR_CUDA_TRY(cudaMemcpy(ts.data(), stamps.p, sizeof(unsigned long long) * ts.size(), cudaMemcpyDeviceToHost));
-    double mx = 0.0, mean = 0.0;
     achr_batch_stats bs{};
     for (int k = 0; k < n_models; ++k) {
-        const float mk = (float)((double)(ts[(size_t)k] - ts[(size_t)n_models]) * 1e-6);
+        const float mk = n_points[k] > 0 ? (float)((double)(ts[(size_t)k] - ts[(size_t)n_models]) * 1e-6) : 0.0f;
         if (model_ms_out) model_ms_out[k] = mk;
-        mx = std::max(mx, (double)mk);
-        mean += mk;
         achr_stats st;
         achr_status r = read_counters(ctxs[k], &st, mk);
         if (r != ACHR_OK) return r;
@@ -1070,9 +1158,17 @@ achr_status achr_sample_batch(achr_ctx *const *ctxs, int32_t n_models, const int
         bs.max_residual = std::max(bs.max_residual, st.max_residual);
         bs.max_bound_violation = std::max(bs.max_bound_violation, st.max_bound_violation);
     }
-    mean /= n_models;
+    // Idle time of the resident CTA slots at the end: the CTAs' exit times
+    // (when each found its queue empty) against the last one.
+    double cmax = 0.0, cmean = 0.0;
+    for (size_t c = 0; c < n_ctas; ++c) {
+        const double t = (double)(ts[(size_t)n_models + 1 + c] - ts[(size_t)n_models]) * 1e-6;
+        cmax = std::max(cmax, t);
+        cmean += t;
+    }
+    if (n_ctas) cmean /= (double)n_ctas;
     bs.graph_ms = total_ms;
-    bs.load_imbalance = mx > 0 ? (mx - mean) / mx : 0.0;
+    bs.load_imbalance = cmax > 0 ? (cmax - cmean) / cmax : 0.0;
     if (stats) *stats = bs;
     return ACHR_OK;
 }

@@ -16,4 +16,14 @@ cudaError_t launch_chain_cfg_mid(int bd, int ept, const ChainArgs &a, cudaStream
     }
 }
 
+cudaError_t launch_chain_queue_mid(int bd, int ept, const ChainQueue &q, cudaStream_t s, int grid, int *per_sm) {
+    switch (bd * 100 + ept) {
+        case 320 * 100 + 12: return launch_queue_cfg<320, 12>(q, s, grid, per_sm);
+        case 384 * 100 + 10: return launch_queue_cfg<384, 10>(q, s, grid, per_sm);
+        case 512 * 100 + 12: return launch_queue_cfg<512, 12>(q, s, grid, per_sm);
+        case 512 * 100 + 15: return launch_queue_cfg<512, 15>(q, s, grid, per_sm);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
 }  // namespace achr

@@ -452,13 +452,31 @@ __host__ __device__ inline size_t chain_smem_bytes_cfg(int np, int d, int bd) {
     return sizeof(double) * 3 * (size_t)np + sizeof(StepEntry) * kTbl + 2 * sizeof(RedSlots) + 128;
 }
 
+// Shared-memory header of a CTA: x, A and the staging buffer (3 NP doubles),
+// the step table, two reduction slots, then the column barrier, eight
+// statistics counters, the exact-evaluation count (two ints), the `never`
+// barrier and the two worst-case words.
+template <int NP>
+__device__ __forceinline__ void chain_barriers(unsigned char *smem_raw, uint64_t *&bar, uint64_t *&never) {
+    RedSlots *rsb = reinterpret_cast<RedSlots *>(reinterpret_cast<StepEntry *>(reinterpret_cast<double *>(smem_raw) +
+                                                                               3 * (size_t)NP) +
+                                                 kTbl);
+    bar = reinterpret_cast<uint64_t *>(rsb + 2);
+    never = reinterpret_cast<uint64_t *>(reinterpret_cast<int *>(bar + 1 + 8) + 2);
+}
+
+// One CTA's share of a launch: chains p_begin, p_begin + p_step, ... below
+// p_end of the model `a` describes, then the CTA's statistics into
+// a.counters.  The staging barriers live in the shared-memory header; the
+// caller initialises them once per CTA and `phase` carries their parity from
+// one call to the next.  Returns true when a bounded wait ran out.
 // SEG: segmented launches of the deferred reprojection (a separate
 // instantiation, so the plain kernel carries none of its code or registers).
 template <int BD, int EPT, bool SEG>
-__global__ void __launch_bounds__(BD, (BD <= 384 ? 2 : 1)) achr_chain_kernel(const ChainArgs a) {
+__device__ __forceinline__ bool chain_run(const ChainArgs &a, int p_begin, int p_step, int p_end,
+                                          unsigned char *smem_raw, unsigned &phase) {
     constexpr int NP = BD * EPT;
     constexpr int NW = BD / 32;
-    extern __shared__ __align__(128) unsigned char smem_raw[];
     const int tid = threadIdx.x;
     const int lane = tid & 31, warp = tid >> 5;
     double *xs = reinterpret_cast<double *>(smem_raw);
@@ -467,19 +485,16 @@ __global__ void __launch_bounds__(BD, (BD <= 384 ? 2 : 1)) achr_chain_kernel(con
     double *ys = ws;  // reprojection scratch (d <= n entries, below the zero padding of ws)
     StepEntry *tbl = reinterpret_cast<StepEntry *>(ws + NP);
     RedSlots *rsb = reinterpret_cast<RedSlots *>(tbl + kTbl);
-    uint64_t *bar = reinterpret_cast<uint64_t *>(rsb + 2);
+    uint64_t *bar, *never;  // the staged column's barrier; a barrier nothing arrives on
+    chain_barriers<NP>(smem_raw, bar, never);
     unsigned long long *cnt = reinterpret_cast<unsigned long long *>(bar + 1);  // CTA statistics, CNT_* slots
     int *exact_count = reinterpret_cast<int *>(cnt + 8);
-    uint64_t *never = reinterpret_cast<uint64_t *>(exact_count + 2);  // a barrier nothing arrives on
     // largest residual and bound violation of the CTA's emitted points (bits of non-negative doubles)
     unsigned long long *worst = reinterpret_cast<unsigned long long *>(never + 1);
     // (S S^T)^+ r of the residual-form reprojection (m floats), when enabled
     float *zs = reinterpret_cast<float *>(smem_raw + chain_smem_bytes_cfg(NP, a.d, BD));
 
     if (tid == 0) {
-        mbar_init(bar, 1);
-        mbar_init(never, 1);
-        fence_mbar_init();
         *exact_count = 0;
         for (int c = 0; c < 8; ++c) cnt[c] = 0;
         worst[0] = worst[1] = 0;
@@ -498,12 +513,12 @@ __global__ void __launch_bounds__(BD, (BD <= 384 ? 2 : 1)) achr_chain_kernel(con
     const bool tail_live = warp * 32 + (EPT - 1) * BD < a.n;
 // (Not for 32 elements per thread, where the branches cost more registers than they save.)
 #define ACHR_PAD_SLOT(k) (EPT < 32 && (k) == EPT - 1 && !tail_live)
-    unsigned phase = 0, it = 0;
+    unsigned it = 0;
     bool failed = false;
 
     // (Scalars that stay constant over a launch are read from the kernel
     // parameters where they are used rather than held in registers.)
-    for (int p = blockIdx.x; p < a.P && !failed; p = (int)min((long long)p + gridDim.x, (long long)a.P)) {
+    for (int p = p_begin; p < p_end && !failed; p = (int)min((long long)p + p_step, (long long)p_end)) {
 #define ACHR_CHAIN_ID (a.chain_offset + (unsigned long long)p)
         // Segmented sampling: the chain's state bits from the earlier launches.
         const unsigned sflags = SEG ? a.seg_flags[p] : 0u;
@@ -1224,6 +1239,71 @@ __global__ void __launch_bounds__(BD, (BD <= 384 ? 2 : 1)) achr_chain_kernel(con
         if (worst[1]) atomicMax(c + CNT_MAXVIOL_BITS, worst[1]);
         if (failed) atomicOr(c + CNT_ERROR, ERR_TMA_TIMEOUT);
     }
+    return failed;
+}
+
+// The staging barriers of a CTA (header of the dynamic shared memory).
+template <int NP>
+__device__ __forceinline__ void chain_init_barriers(unsigned char *smem_raw) {
+    uint64_t *bar, *never;
+    chain_barriers<NP>(smem_raw, bar, never);
+    if (threadIdx.x == 0) {
+        mbar_init(bar, 1);
+        mbar_init(never, 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+}
+
+// One model: CTA b takes chains b, b + grid, ...
+template <int BD, int EPT, bool SEG>
+__global__ void __launch_bounds__(BD, (BD <= 384 ? 2 : 1)) achr_chain_kernel(const ChainArgs a) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    chain_init_barriers<BD * EPT>(smem_raw);
+    unsigned phase = 0;
+    chain_run<BD, EPT, SEG>(a, blockIdx.x, gridDim.x, a.P, smem_raw, phase);
+}
+
+// Many models of one configuration in one persistent launch: each CTA takes
+// the next (model, first chain, end chain) item of a device work queue until
+// the queue is empty.  The host orders the items longest model first, with
+// tiles that shrink towards the end of the queue, and sets the residual-form
+// reprojection off (its shared memory is not part of this launch).  When a
+// model's last chain is done, its finish time (globaltimer, ns) goes to
+// done_ns[model].
+template <int BD, int EPT>
+__global__ void __launch_bounds__(BD, (BD <= 384 ? 2 : 1)) achr_chain_queue_kernel(const ChainQueue q) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    __shared__ ChainArgs sa;
+    __shared__ int4 cur;
+    static_assert(sizeof(ChainArgs) % sizeof(int) == 0, "ChainArgs is copied as 32-bit words");
+    chain_init_barriers<BD * EPT>(smem_raw);
+    unsigned phase = 0;
+    int model = -1;
+    for (;;) {
+        if (threadIdx.x == 0) {
+            const int k = atomicAdd(q.next, 1);
+            cur = k < q.n_items ? q.items[k] : make_int4(-1, 0, 0, 0);
+        }
+        __syncthreads();
+        const int4 item = cur;
+        if (item.x < 0) break;
+        if (item.x != model) {
+            const int *src = reinterpret_cast<const int *>(q.args + item.x);
+            int *dst = reinterpret_cast<int *>(&sa);
+            for (int w = threadIdx.x; w < (int)(sizeof(ChainArgs) / sizeof(int)); w += BD) dst[w] = src[w];
+            model = item.x;
+        }
+        __syncthreads();
+        const bool failed = chain_run<BD, EPT, false>(sa, item.y, 1, item.z, smem_raw, phase);
+        if (threadIdx.x == 0) {
+            const int n = item.z - item.y;
+            if (atomicAdd(q.chains_done + item.x, n) + n == sa.P) q.done_ns[item.x] = global_ns();
+        }
+        if (failed) break;  // recorded in the model's counters; the CTA stops taking work
+        __syncthreads();    // `cur` and `sa` are rewritten only after every thread is done with them
+    }
+    if (threadIdx.x == 0 && q.cta_ns) q.cta_ns[blockIdx.x] = global_ns();
 }
 
 // Occupancy-sized persistent launch of one configuration.  max_ctas > 0 caps
@@ -1266,6 +1346,31 @@ cudaError_t launch_cfg_kernel(const ChainArgs &a_in, cudaStream_t stream, int ma
     if (grid > a.P) grid = a.P;
     if (grid < 1) return cudaSuccess;
     KFN<<<(unsigned)grid, BD, smem, stream>>>(a);
+    return cudaGetLastError();
+}
+
+// Persistent work-queue launch of one configuration: `grid` CTAs (0: every
+// resident slot of the GPU), with q.extra_smem bytes of shared memory beyond
+// the header for the residual-form reprojection.  per_sm_out (if non-NULL)
+// receives the CTAs that fit on one SM; with q.n_items = 0 nothing is launched.
+template <int BD, int EPT>
+cudaError_t launch_queue_cfg(const ChainQueue &q, cudaStream_t stream, int grid, int *per_sm_out) {
+    auto *const KFN = achr_chain_queue_kernel<BD, EPT>;
+    const size_t smem = chain_smem_bytes_cfg(BD * EPT, 0, BD) + q.extra_smem;
+    cudaError_t e = cudaFuncSetAttribute(KFN, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    int per_sm = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, KFN, BD, smem);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1) return cudaErrorInvalidConfiguration;
+    if (per_sm_out) *per_sm_out = per_sm;
+    if (q.n_items <= 0) return cudaSuccess;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    long long g = grid > 0 ? grid : (long long)sms * per_sm;
+    if (g > q.n_items) g = q.n_items;
+    KFN<<<(unsigned)g, BD, smem, stream>>>(q);
     return cudaGetLastError();
 }
 

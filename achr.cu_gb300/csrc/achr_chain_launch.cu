@@ -11,6 +11,9 @@ namespace achr {
 cudaError_t launch_chain_cfg_small(int bd, int ept, const ChainArgs &a, cudaStream_t s, int max_ctas, int *per_sm);
 cudaError_t launch_chain_cfg_large(int bd, int ept, const ChainArgs &a, cudaStream_t s, int max_ctas, int *per_sm);
 cudaError_t launch_chain_cfg_mid(int bd, int ept, const ChainArgs &a, cudaStream_t s, int max_ctas, int *per_sm);
+cudaError_t launch_chain_queue_small(int bd, int ept, const ChainQueue &q, cudaStream_t s, int grid, int *per_sm);
+cudaError_t launch_chain_queue_mid(int bd, int ept, const ChainQueue &q, cudaStream_t s, int grid, int *per_sm);
+cudaError_t launch_chain_queue_large(int bd, int ept, const ChainQueue &q, cudaStream_t s, int grid, int *per_sm);
 
 namespace {
 
@@ -78,6 +81,21 @@ size_t chain_smem_bytes(int n, int d, int ldw, int block) {
     (void)d;
     const int np = chain_padded_length(n, block);
     return sizeof(double) * 3 * (size_t)np + 24 * 64 + 2 * 1792 + 128;
+}
+
+bool chain_config(int n, int threads_per_chain, int *bd, int *ept) {
+    const Cfg *c = find_cfg(n, threads_per_chain);
+    if (!c) return false;
+    *bd = c->bd;
+    *ept = c->ept;
+    return true;
+}
+
+cudaError_t launch_chain_queue(int bd, int ept, const ChainQueue &q, cudaStream_t stream, int grid, int *per_sm) {
+    if (bd <= 128) return launch_chain_queue_small(bd, ept, q, stream, grid, per_sm);
+    if (bd == 320 || bd == 384 || (bd == 512 && (ept == 12 || ept == 15)))
+        return launch_chain_queue_mid(bd, ept, q, stream, grid, per_sm);
+    return launch_chain_queue_large(bd, ept, q, stream, grid, per_sm);
 }
 
 cudaError_t launch_chains(const ChainArgs &a, int threads_per_chain, cudaStream_t stream, int max_ctas,

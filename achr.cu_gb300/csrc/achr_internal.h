@@ -103,6 +103,19 @@ struct ChainArgs {
     const float *seg_dxh, *seg_dxl;  // P x ld_seg: the passes' correction (double-float), subtracted next launch
 };
 
+// Work queue of a persistent multi-model launch (achr_chain_queue_kernel):
+// items (model, first chain, end chain) taken in order by the CTAs.
+struct ChainQueue {
+    const ChainArgs *args;        // one per model (device)
+    const int4 *items;            // (model, p0, p1, 0)
+    int n_items;
+    int *next;                    // the next item to take (zero before the launch)
+    int *chains_done;             // per model, zero before the launch
+    unsigned long long *done_ns;  // per model: globaltimer when its last chain finished
+    size_t extra_smem;            // shared memory for (S S^T)^+ r (m floats) of the residual-form models
+    unsigned long long *cta_ns;   // NULL or one per CTA: globaltimer when the CTA found the queue empty
+};
+
 // Per-chain state bits of segmented sampling.
 enum SegFlag : unsigned {
     SEG_STARTED = 1u,   // the chain-major state holds the chain's point and accumulator
@@ -149,6 +162,10 @@ cudaError_t launch_chains(const ChainArgs &a, int threads_per_chain, cudaStream_
 // Configuration ladder: threads per chain and padded element count for n
 // reactions (threads_per_chain = 0: default); 0 if no configuration fits.
 int chain_block_size(int n, int threads_per_chain);
+// Configuration (threads, elements per thread) the model of n reactions runs with.
+bool chain_config(int n, int threads_per_chain, int *bd, int *ept);
+// Persistent work-queue launch of the configuration (bd, ept); see ChainQueue.
+cudaError_t launch_chain_queue(int bd, int ept, const ChainQueue &q, cudaStream_t stream, int grid, int *per_sm);
 int chain_padded_length(int n, int threads_per_chain);
 // Length to pad per-reaction arrays to: twice the default padded length (so
 // every autotuning candidate fits), at most 16384.

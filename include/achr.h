@@ -375,21 +375,28 @@ achr_status achr_autotune(achr_ctx *ctx, int32_t *threads_per_chain_out);
 
 typedef struct {
     double graph_ms;            /* device time of the whole batched launch */
-    double load_imbalance;      /* (max - mean) / max over the models' finish times */
+    double load_imbalance;      /* (max - mean) / max over the CTAs' exit times (from the launch):
+                                   the share of the resident CTA slots left idle at the end */
     int64_t accepted, rejected, reprojections, stuck_chains;
     double max_residual, max_bound_violation;
 } achr_batch_stats;
 
-/* Sample several models at once: one CUDA graph launch holding one chain
- * kernel per model, each on its own stream, one CTA per chain, launched in
- * order of predicted time (from the throughput achr_autotune measured for the
- * model, else chains x steps x padded reactions) so that the hardware CTA
- * scheduler keeps every SM busy until the last chains finish.  Model k runs
- * n_points[k] chains of n_steps into d_points_out[k] (device, n_k x P_k,
- * leading dimension ld_out[k]); its chain ids start at the sum of the earlier
- * models' n_points, so achr_sample_device on model k alone with that
- * chain_offset gives the same points.  Synchronises `stream`; per-model finish
- * times (ms from the launch) go to model_ms_out[k] if non-NULL. */
+/* Sample several models at once in one CUDA-graph launch.  Models are grouped
+ * by chain-kernel configuration (threads per chain x reactions per thread,
+ * from the context's options, e.g. as achr_autotune chose them); each group is
+ * one persistent kernel, one CTA per resident slot of the GPU, whose CTAs take
+ * (model, first chain, end chain) items from a device work queue until it is
+ * empty.  Items run in order of predicted chain time (the throughput
+ * achr_autotune measured for the model, else steps x padded reactions),
+ * longest model first, and each item holds about a quarter of the work still
+ * queued behind it over the CTAs, so the tiles shrink to single chains at the
+ * end of the queue.  Groups run on their own streams, largest total work
+ * first.  Model k runs n_points[k] chains of n_steps into d_points_out[k]
+ * (device, n_k x P_k, leading dimension ld_out[k]); its chain ids start at the
+ * sum of the earlier models' n_points, so achr_sample_device on model k alone
+ * with that chain_offset gives the same points.  Synchronises `stream`;
+ * per-model finish times (ms from the launch) go to model_ms_out[k] if
+ * non-NULL. */
 achr_status achr_sample_batch(achr_ctx *const *ctxs, int32_t n_models, const int32_t *n_points, int32_t n_steps,
                               uint64_t seed, double *const *d_points_out, const int64_t *ld_out, void *stream,
                               achr_batch_stats *stats, double *model_ms_out);

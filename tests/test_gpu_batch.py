@@ -1,4 +1,10 @@
-"""GPU: batched sampling of several models in one CUDA-graph launch, and the autotuner."""
+"""GPU: batched sampling of several models in one CUDA-graph launch, and the autotuner.
+
+achr_sample_batch groups the models by chain-kernel configuration and runs
+each group as one persistent kernel whose CTAs take (model, chain tile) items
+from a device work queue; every chain must come out exactly as the same chain
+sampled on its own (same seed, chain id = the model's offset in the batch).
+"""
 from __future__ import annotations
 
 import importlib
@@ -72,3 +78,44 @@ def test_autotune_picks_a_candidate_and_keeps_parity(pkg, models, oracle_mod):
     ref, rst = oracle_mod.sample(m, w, N, 3, 20, 30)
     assert np.abs(pts - ref).max() <= REL_TOL * max(1.0, np.abs(ref).max())
     assert st["accepted"] == rst["accepted"]
+
+
+@pytest.fixture(scope="module")
+def queue_models(pkg, models):
+    """The three models above plus one of 1500 reactions (a fourth configuration, 256 x 8) and the
+    72 x 95 fixture once more, so that one queue holds three models."""
+    synth = importlib.import_module("achr_gb300.synthetic")
+    from oracle import reference_py
+    spec = synth.batch_spec(7, 1500)
+    row, col, val, lb, ub = synth.make_model(spec)
+    m = pkg.HostModel(spec.n_rxns, spec.n_mets, row, col, val, lb, ub)
+    S = dense_S(m)
+    warm = synth.interior_chord_warmup(S, lb, ub, 2 * spec.n_rxns, seed=spec.seed)
+    return models + [(m, warm, reference_py.null_space_sts(S)), models[0]]
+
+
+def test_batch_work_queue_many_tiles(pkg, queue_models):
+    """Enough chains that the queues cut each model into tiles of several sizes, a model with no
+    chains, two models sharing one configuration with a third: bitwise equal to separate runs."""
+    torch = pytest.importorskip("torch")
+    samplers = []
+    for m, w, N in queue_models:
+        s = pkg.Sampler(m, w)
+        s.set_null_space(N)
+        samplers.append(s)
+    P = [3000, 700, 0, 450, 1234]
+    T = 23
+    outs = [torch.zeros((s.n, max(p, 1)), dtype=torch.float64, device="cuda") for s, p in zip(samplers, P)]
+    stream = torch.cuda.current_stream().cuda_stream
+    st, ms = pkg.sample_batch(samplers, P, T, [o.data_ptr() for o in outs], [max(p, 1) for p in P], stream=stream,
+                              seed=4242)
+    assert st["accepted"] == sum(P) * T and st["stuck_chains"] == 0
+    assert 0.0 <= st["load_imbalance"] < 1.0 and ms[2] == 0.0 and min(ms[k] for k in (0, 1, 3, 4)) > 0.0
+    off = 0
+    for s, p, o in zip(samplers, P, outs):
+        if p:
+            ref, _ = s.sample(p, T, seed=4242, chain_offset=off)
+            assert np.array_equal(o[:, :p].cpu().numpy(), ref)
+        off += p
+    for s in samplers:
+        s.close()
