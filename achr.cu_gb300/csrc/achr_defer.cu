@@ -215,18 +215,76 @@ __device__ __forceinline__ float block_max(float v, float *red) {
     return m;
 }
 
+// Shared-memory floats per chain of the pass kernels (multiples of 4, so every
+// chain's block starts on a 16-byte boundary): z (ldz floats) and d, as a
+// double-float pair in the first pass, in FP32 in the later ones.
+__host__ __device__ inline size_t pass1_floats(long long ldz, long long ld) {
+    return ((size_t)ldz + 2 * (size_t)ld + 3) & ~(size_t)3;
+}
+__host__ __device__ inline size_t pass_floats(long long ldz, long long ld) {
+    return ((size_t)ldz + (size_t)ld + 3) & ~(size_t)3;
+}
+
+// The kernels below are bound by latency, not by bandwidth or arithmetic: each
+// sparse slot is a global load of its index and value followed by a shared-
+// memory gather, and each per-chain vector moves between global and shared
+// memory.  So every loop issues a batch of independent loads before it uses
+// any of them: kSlots slots of a sparse line, and two elements per thread of
+// every resident chain's vectors.
+constexpr int kSlots = 8;
+
+// z rows of the CTA's live chains into shared memory (float4 copies).
+template <int CPB>
+__device__ __forceinline__ void stage_z(const PassArgs &a, int p0, const int *live, float *sm, size_t per) {
+    const int q4 = (int)(a.ldz >> 2);
+    for (int i0 = 0; i0 < q4; i0 += 2 * kPassThreads) {
+        float4 v[CPB][2];
+#pragma unroll
+        for (int c = 0; c < CPB; ++c)
+#pragma unroll
+            for (int u = 0; u < 2; ++u) {
+                const int i = i0 + u * kPassThreads + (int)threadIdx.x;
+                v[c][u] = (live[c] && i < q4)
+                              ? __ldg(reinterpret_cast<const float4 *>(a.Z + (size_t)(p0 + c) * (size_t)a.ldz) + i)
+                              : make_float4(0.f, 0.f, 0.f, 0.f);
+            }
+#pragma unroll
+        for (int c = 0; c < CPB; ++c)
+#pragma unroll
+            for (int u = 0; u < 2; ++u) {
+                const int i = i0 + u * kPassThreads + (int)threadIdx.x;
+                if (live[c] && i < q4) reinterpret_cast<float4 *>(sm + c * per)[i] = v[c][u];
+            }
+    }
+}
+
+// Slots [t0, t0 + kSlots) of the line lane `lane` of group g holds: indices and
+// values (out-of-range slots read the line's last slot with value 0, which
+// adds exactly nothing).
+template <bool LO>
+__device__ __forceinline__ void load_slots(const EllView &E, int base, int len, int t0, int lane, int *ii, float *hh,
+                                           float *ll) {
+#pragma unroll
+    for (int u = 0; u < kSlots; ++u) {
+        const int t = t0 + u;
+        const int q = base + (min(t, len - 1) << 5) + lane;
+        ii[u] = __ldg(E.idx + q);
+        hh[u] = t < len ? __ldg(E.vh + q) : 0.0f;
+        if (LO) ll[u] = t < len ? __ldg(E.vl + q) : 0.0f;
+    }
+}
+
 // The first pass, in double-float, for CPB chains at a time per CTA (the
 // sparse structure each warp loads serves all of them): for every chain
 // flagged SEG_REPROJ, d = S^T z (z the chain's GEMM row), dx = d, and
 // r = r0 - S d from the chain kernel's FP64 r0; r goes on in FP32 (r) and as
-// the next GEMM's BF16 split.  Shared memory per chain: z (ldz floats), d as
-// hi and lo (2 ld floats).
+// the next GEMM's BF16 split.
 template <int CPB, bool EXACT32>
 __global__ void __launch_bounds__(kPassThreads) defer_pass1_kernel(const PassArgs a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ float red[kPassWarps];
     __shared__ int live[CPB];
-    const size_t per = (size_t)a.ldz + 2 * (size_t)a.ld;
+    const size_t per = pass1_floats(a.ldz, a.ld);
     float *const sm = reinterpret_cast<float *>(smem_raw);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     if (*a.this_gate == 0ull) return;  // no chain's check fired (the GEMM did not run either)
@@ -241,42 +299,37 @@ __global__ void __launch_bounds__(kPassThreads) defer_pass1_kernel(const PassArg
             __syncthreads();
             continue;
         }
-#pragma unroll
-        for (int c = 0; c < CPB; ++c) {
-            if (!live[c]) continue;
-            const float *zp = a.Z + (size_t)(p0 + c) * (size_t)a.ldz;
-            float *zs = sm + c * per;
-            for (int i = tid; i < a.m; i += kPassThreads) zs[i] = zp[i];
-        }
+        stage_z<CPB>(a, p0, live, sm, per);
         __syncthreads();
+        // d = S^T z, one line (column of S) per lane
         for (int g = warp; g < a.cols.groups; g += kPassWarps) {
             const int base = __ldg(a.cols.off + g);
             const int len = (__ldg(a.cols.off + g + 1) - base) >> 5;
+            const int j = __ldg(a.cols.line + (g << 5) + lane);
             float ah[CPB], al[CPB];
 #pragma unroll
             for (int c = 0; c < CPB; ++c) ah[c] = al[c] = 0.0f;
-#pragma unroll 2
-            for (int t = 0; t < len; ++t) {
-                const int q = base + (t << 5) + lane;
-                const int i = __ldg(a.cols.idx + q);
-                const float sh = __ldg(a.cols.vh + q);
-                const float sl = EXACT32 ? 0.0f : __ldg(a.cols.vl + q);
+            for (int t0 = 0; t0 < len; t0 += kSlots) {
+                int ii[kSlots];
+                float hh[kSlots], ll[kSlots];
+                load_slots<!EXACT32>(a.cols, base, len, t0, lane, ii, hh, ll);
 #pragma unroll
-                for (int c = 0; c < CPB; ++c) {
-                    const float z = sm[c * per + i];
-                    float ph, pe, s, e;
-                    two_prod(sh, z, ph, pe);
-                    if (!EXACT32) pe = fmaf(sl, z, pe);
-                    two_sum(ah[c], ph, s, e);
-                    ah[c] = s;
-                    al[c] = __fadd_rn(al[c], __fadd_rn(e, pe));
+                for (int u = 0; u < kSlots; ++u) {
+#pragma unroll
+                    for (int c = 0; c < CPB; ++c) {
+                        const float z = sm[c * per + ii[u]];
+                        float ph, pe, s, e;
+                        two_prod(hh[u], z, ph, pe);
+                        if (!EXACT32) pe = fmaf(ll[u], z, pe);
+                        two_sum(ah[c], ph, s, e);
+                        ah[c] = s;
+                        al[c] = __fadd_rn(al[c], __fadd_rn(e, pe));
+                    }
                 }
             }
-            const int j = __ldg(a.cols.line + (g << 5) + lane);
             if (j >= 0) {
 #pragma unroll
                 for (int c = 0; c < CPB; ++c) {
-                    if (!live[c]) continue;
                     float h, l;
                     fast_two_sum(ah[c], al[c], h, l);
                     float *dh = sm + c * per + a.ldz;
@@ -297,37 +350,47 @@ __global__ void __launch_bounds__(kPassThreads) defer_pass1_kernel(const PassArg
                 gl[j] = dh[a.ld + j];
             }
         }
+        // r = r0 - S d, one line (row of S, device order: line q is row q) per lane
         float mx[CPB], m0[CPB];
 #pragma unroll
         for (int c = 0; c < CPB; ++c) mx[c] = m0[c] = 0.0f;
         for (int g = warp; g < a.rows.groups; g += kPassWarps) {
             const int i = __ldg(a.rows.line + (g << 5) + lane);
-            float ah[CPB], al[CPB];
+            double r0d[CPB];
 #pragma unroll
-            for (int c = 0; c < CPB; ++c) {
-                ah[c] = al[c] = 0.0f;
-                if (i >= 0 && live[c]) split_f64(a.rd[(size_t)(p0 + c) * (size_t)a.ldz + (size_t)i], ah[c], al[c]);
-                m0[c] = fmaxf(m0[c], fabsf(ah[c]));
-            }
+            for (int c = 0; c < CPB; ++c)
+                r0d[c] = (i >= 0 && live[c]) ? a.rd[(size_t)(p0 + c) * (size_t)a.ldz + (size_t)i] : 0.0;
             const int base = __ldg(a.rows.off + g);
             const int len = (__ldg(a.rows.off + g + 1) - base) >> 5;
-#pragma unroll 2
-            for (int t = 0; t < len; ++t) {
-                const int q = base + (t << 5) + lane;
-                const int j = __ldg(a.rows.idx + q);
-                const float sh = __ldg(a.rows.vh + q);
-                const float sl = EXACT32 ? 0.0f : __ldg(a.rows.vl + q);
+            float ah[CPB], al[CPB];
+            bool init = false;
+            for (int t0 = 0; t0 < len || !init; t0 += kSlots) {
+                int ii[kSlots];
+                float hh[kSlots], ll[kSlots];
+                if (t0 < len) load_slots<!EXACT32>(a.rows, base, len, t0, lane, ii, hh, ll);
+                if (!init) {  // the FP64 residual, split once its load has had the slot loads to hide behind
 #pragma unroll
-                for (int c = 0; c < CPB; ++c) {
-                    const float *dh = sm + c * per + a.ldz;
-                    const float xh = dh[j], xl = dh[a.ld + j];
-                    float ph, pe, s, e;
-                    two_prod(sh, xh, ph, pe);
-                    pe = fmaf(sh, xl, pe);
-                    if (!EXACT32) pe = fmaf(sl, xh, pe);
-                    two_sum(ah[c], -ph, s, e);
-                    ah[c] = s;
-                    al[c] = __fadd_rn(al[c], __fsub_rn(e, pe));
+                    for (int c = 0; c < CPB; ++c) {
+                        split_f64(r0d[c], ah[c], al[c]);
+                        m0[c] = fmaxf(m0[c], fabsf(ah[c]));
+                    }
+                    init = true;
+                }
+                if (t0 >= len) break;
+#pragma unroll
+                for (int u = 0; u < kSlots; ++u) {
+#pragma unroll
+                    for (int c = 0; c < CPB; ++c) {
+                        const float *dh = sm + c * per + a.ldz;
+                        const float xh = dh[ii[u]], xl = dh[a.ld + ii[u]];
+                        float ph, pe, s, e;
+                        two_prod(hh[u], xh, ph, pe);
+                        pe = fmaf(hh[u], xl, pe);
+                        if (!EXACT32) pe = fmaf(ll[u], xh, pe);
+                        two_sum(ah[c], -ph, s, e);
+                        ah[c] = s;
+                        al[c] = __fadd_rn(al[c], __fsub_rn(e, pe));
+                    }
                 }
             }
             if (i >= 0) {
@@ -361,13 +424,13 @@ __global__ void __launch_bounds__(kPassThreads) defer_pass1_kernel(const PassArg
 
 // A later pass (pass >= 1), in FP32, for CPB chains at a time per CTA: for
 // every chain still flagged SEG_REPROJ, d = S^T z, dx += d (double-float),
-// r <- r - S d.  Shared memory per chain: z (ldz floats), d (ld floats).
+// r <- r - S d.
 template <int CPB>
 __global__ void __launch_bounds__(kPassThreads) defer_pass_kernel(const PassArgs a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ float red[kPassWarps];
     __shared__ int live[CPB];
-    const size_t per = (size_t)a.ldz + (size_t)a.ld;
+    const size_t per = pass_floats(a.ldz, a.ld);
     float *const sm = reinterpret_cast<float *>(smem_raw);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     if (*a.this_gate == 0ull) return;  // no chain needed this pass (its GEMM did not run either)
@@ -382,73 +445,85 @@ __global__ void __launch_bounds__(kPassThreads) defer_pass_kernel(const PassArgs
             __syncthreads();
             continue;
         }
-#pragma unroll
-        for (int c = 0; c < CPB; ++c) {
-            if (!live[c]) continue;
-            const float *zp = a.Z + (size_t)(p0 + c) * (size_t)a.ldz;
-            float *zs = sm + c * per;
-            for (int i = tid; i < a.m; i += kPassThreads) zs[i] = zp[i];
-        }
+        stage_z<CPB>(a, p0, live, sm, per);
         __syncthreads();
         for (int g = warp; g < a.cols.groups; g += kPassWarps) {
             const int base = __ldg(a.cols.off + g);
             const int len = (__ldg(a.cols.off + g + 1) - base) >> 5;
+            const int j = __ldg(a.cols.line + (g << 5) + lane);
             float d[CPB];
 #pragma unroll
             for (int c = 0; c < CPB; ++c) d[c] = 0.0f;
-#pragma unroll 4
-            for (int t = 0; t < len; ++t) {
-                const int q = base + (t << 5) + lane;
-                const int i = __ldg(a.cols.idx + q);
-                const float sh = __ldg(a.cols.vh + q);
+            for (int t0 = 0; t0 < len; t0 += kSlots) {
+                int ii[kSlots];
+                float hh[kSlots];
+                load_slots<false>(a.cols, base, len, t0, lane, ii, hh, nullptr);
 #pragma unroll
-                for (int c = 0; c < CPB; ++c) d[c] = fmaf(sh, sm[c * per + i], d[c]);
+                for (int u = 0; u < kSlots; ++u)
+#pragma unroll
+                    for (int c = 0; c < CPB; ++c) d[c] = fmaf(hh[u], sm[c * per + ii[u]], d[c]);
             }
-            const int j = __ldg(a.cols.line + (g << 5) + lane);
             if (j >= 0) {
 #pragma unroll
-                for (int c = 0; c < CPB; ++c)
-                    if (live[c]) sm[c * per + a.ldz + j] = d[c];
+                for (int c = 0; c < CPB; ++c) sm[c * per + a.ldz + j] = d[c];
             }
         }
         __syncthreads();
         // dx += d in reaction order (the lines above run in column-length order)
+        for (int j0 = 0; j0 < a.n; j0 += 2 * kPassThreads) {
+            float h[CPB][2], l[CPB][2];
 #pragma unroll
-        for (int c = 0; c < CPB; ++c) {
-            if (!live[c]) continue;
-            const float *ds = sm + c * per + a.ldz;
-            float *gh = a.dxh + (size_t)(p0 + c) * (size_t)a.ld, *gl = a.dxl + (size_t)(p0 + c) * (size_t)a.ld;
-            for (int j = tid; j < a.n; j += kPassThreads) {
-                float s, e;
-                two_sum(gh[j], ds[j], s, e);
-                gh[j] = s;
-                gl[j] = __fadd_rn(gl[j], e);
-            }
+            for (int c = 0; c < CPB; ++c)
+#pragma unroll
+                for (int u = 0; u < 2; ++u) {
+                    const int j = j0 + u * kPassThreads + tid;
+                    const size_t o = (size_t)(p0 + c) * (size_t)a.ld + (size_t)j;
+                    const bool on = live[c] && j < a.n;
+                    h[c][u] = on ? a.dxh[o] : 0.0f;
+                    l[c][u] = on ? a.dxl[o] : 0.0f;
+                }
+#pragma unroll
+            for (int c = 0; c < CPB; ++c)
+#pragma unroll
+                for (int u = 0; u < 2; ++u) {
+                    const int j = j0 + u * kPassThreads + tid;
+                    if (!(live[c] && j < a.n)) continue;
+                    const size_t o = (size_t)(p0 + c) * (size_t)a.ld + (size_t)j;
+                    float s, e;
+                    two_sum(h[c][u], sm[c * per + a.ldz + j], s, e);
+                    a.dxh[o] = s;
+                    a.dxl[o] = __fadd_rn(l[c][u], e);
+                }
         }
         float mx[CPB];
 #pragma unroll
         for (int c = 0; c < CPB; ++c) mx[c] = 0.0f;
         for (int g = warp; g < a.rows.groups; g += kPassWarps) {
+            const int i = __ldg(a.rows.line + (g << 5) + lane);
+            float rold[CPB];
+#pragma unroll
+            for (int c = 0; c < CPB; ++c)
+                rold[c] = (i >= 0 && live[c]) ? a.r[(size_t)(p0 + c) * (size_t)a.ldz + (size_t)i] : 0.0f;
             const int base = __ldg(a.rows.off + g);
             const int len = (__ldg(a.rows.off + g + 1) - base) >> 5;
             float acc[CPB];
 #pragma unroll
             for (int c = 0; c < CPB; ++c) acc[c] = 0.0f;
-#pragma unroll 4
-            for (int t = 0; t < len; ++t) {
-                const int q = base + (t << 5) + lane;
-                const int j = __ldg(a.rows.idx + q);
-                const float sh = __ldg(a.rows.vh + q);
+            for (int t0 = 0; t0 < len; t0 += kSlots) {
+                int ii[kSlots];
+                float hh[kSlots];
+                load_slots<false>(a.rows, base, len, t0, lane, ii, hh, nullptr);
 #pragma unroll
-                for (int c = 0; c < CPB; ++c) acc[c] = fmaf(sh, sm[c * per + a.ldz + j], acc[c]);
+                for (int u = 0; u < kSlots; ++u)
+#pragma unroll
+                    for (int c = 0; c < CPB; ++c) acc[c] = fmaf(hh[u], sm[c * per + a.ldz + ii[u]], acc[c]);
             }
-            const int i = __ldg(a.rows.line + (g << 5) + lane);
             if (i >= 0) {
 #pragma unroll
                 for (int c = 0; c < CPB; ++c) {
                     if (!live[c]) continue;
                     const size_t o = (size_t)(p0 + c) * (size_t)a.ldz + (size_t)i;
-                    const float rn = __fsub_rn(a.r[o], acc[c]);
+                    const float rn = __fsub_rn(rold[c], acc[c]);
                     a.r[o] = rn;
                     mx[c] = fmaxf(mx[c], fabsf(rn));
                     if (!a.last)
@@ -477,7 +552,7 @@ struct PassPlan {
 
 PassPlan plan_passes(long long ld, long long ldz, bool exact32) {
     PassPlan pl{};
-    const size_t per1 = sizeof(float) * ((size_t)ldz + 2 * (size_t)ld), per = sizeof(float) * ((size_t)ldz + (size_t)ld);
+    const size_t per1 = sizeof(float) * pass1_floats(ldz, ld), per = sizeof(float) * pass_floats(ldz, ld);
     pl.cpb1 = per1 * 4 <= kPassSmemMax ? 4 : per1 * 2 <= kPassSmemMax ? 2 : 1;
     pl.cpb = per * 4 <= kPassSmemMax ? 4 : per * 2 <= kPassSmemMax ? 2 : 1;
     pl.smem1 = per1 * (size_t)pl.cpb1;
