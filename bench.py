@@ -85,6 +85,8 @@ def parse_args():
     ap.add_argument("--chains", type=int, default=0, help="override the workload's chain count (0: its own)")
     ap.add_argument("--bracket-pass", type=int, choices=[0, 1], default=0,
                     help="0: ratio-test brackets formed with the direction; 1: a separate pass")
+    ap.add_argument("--reproject-form", type=int, default=None, choices=[0, 1, 2, 3],
+                    help="the library's reprojection form (default: chosen from the inputs)")
     ap.add_argument("--profile-case", type=int, nargs=2, metavar=("CHAINS", "STEPS"),
                     help="run two launches of CHAINS x STEPS of the workload and print their times (ncu captures)")
     return ap.parse_args()
@@ -92,7 +94,10 @@ def parse_args():
 
 def sampler_options(args):
     """Chain-kernel options from the command line (defaults: chosen by the library)."""
-    return {"threads_per_chain": args.threads_per_chain, "bracket_pass": args.bracket_pass}
+    o = {"threads_per_chain": args.threads_per_chain, "bracket_pass": args.bracket_pass}
+    if args.reproject_form is not None:
+        o["reproject_form"] = args.reproject_form
+    return o
 
 
 def dist_info():
