@@ -352,6 +352,17 @@ __device__ __forceinline__ unsigned long long residual_rows(const ChainArgs &a, 
     return mx;
 }
 
+// 0.0 from a volatile asm statement.  A computation that starts from it stays
+// inside the branch that guards it: without it the compiler may compute the
+// FP64 norm of d (one DFMA per element, which almost no step needs) ahead of
+// its branch on every step, as it did in the segmented instantiation (a third
+// more FP64 work per step on the pipe that bounds this kernel).
+__device__ __forceinline__ double fp64_zero_here() {
+    double z;
+    asm volatile("mov.b64 %0, 0;" : "=d"(z));
+    return z;
+}
+
 // FP32 -> FP64 with integer operations only (exact for normal values; zero and
 // subnormal values give a signed zero).
 __device__ __forceinline__ double f32_to_f64_exact(float f) {
@@ -828,7 +839,7 @@ __device__ __forceinline__ bool chain_run(const ChainArgs &a, int p_begin, int p
                 int anyv;
                 for (int b2 = 0;; ++b2) {
                     if ((fl & 4) && !have_norm64) {
-                        double s64 = 0.0;
+                        double s64 = fp64_zero_here();
 #pragma unroll
                         for (int k = 0; k < EPT; ++k) s64 = fma(dreg[k], dreg[k], s64);
 #pragma unroll
@@ -943,7 +954,7 @@ __device__ __forceinline__ bool chain_run(const ChainArgs &a, int p_begin, int p
                     } else if (small) {
                         reject = true;
                     } else {
-                        double s64 = 0.0;
+                        double s64 = fp64_zero_here();
 #pragma unroll
                         for (int k = 0; k < EPT; ++k) s64 = fma(dreg[k], dreg[k], s64);
 #pragma unroll
