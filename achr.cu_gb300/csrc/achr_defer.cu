@@ -258,19 +258,19 @@ __device__ __forceinline__ void stage_z(const PassArgs &a, int p0, const int *li
     }
 }
 
-// Slots [t0, t0 + kSlots) of the line lane `lane` of group g holds: indices and
-// values (out-of-range slots read the line's last slot with value 0, which
-// adds exactly nothing).
+// Slots [t0, min(t0 + kSlots, len)) of the line lane `lane` of a group holds:
+// indices and values, all loads issued before any is used.
 template <bool LO>
 __device__ __forceinline__ void load_slots(const EllView &E, int base, int len, int t0, int lane, int *ii, float *hh,
                                            float *ll) {
 #pragma unroll
     for (int u = 0; u < kSlots; ++u) {
         const int t = t0 + u;
-        const int q = base + (min(t, len - 1) << 5) + lane;
+        if (t >= len) break;  // the warp's line length: a uniform branch
+        const int q = base + (t << 5) + lane;
         ii[u] = __ldg(E.idx + q);
-        hh[u] = t < len ? __ldg(E.vh + q) : 0.0f;
-        if (LO) ll[u] = t < len ? __ldg(E.vl + q) : 0.0f;
+        hh[u] = __ldg(E.vh + q);
+        if (LO) ll[u] = __ldg(E.vl + q);
     }
 }
 
@@ -315,6 +315,7 @@ __global__ void __launch_bounds__(kPassThreads) defer_pass1_kernel(const PassArg
                 load_slots<!EXACT32>(a.cols, base, len, t0, lane, ii, hh, ll);
 #pragma unroll
                 for (int u = 0; u < kSlots; ++u) {
+                    if (t0 + u >= len) break;  // (len is the warp's: a uniform branch)
 #pragma unroll
                     for (int c = 0; c < CPB; ++c) {
                         const float z = sm[c * per + ii[u]];
@@ -379,6 +380,7 @@ __global__ void __launch_bounds__(kPassThreads) defer_pass1_kernel(const PassArg
                 if (t0 >= len) break;
 #pragma unroll
                 for (int u = 0; u < kSlots; ++u) {
+                    if (t0 + u >= len) break;
 #pragma unroll
                     for (int c = 0; c < CPB; ++c) {
                         const float *dh = sm + c * per + a.ldz;
@@ -426,7 +428,7 @@ __global__ void __launch_bounds__(kPassThreads) defer_pass1_kernel(const PassArg
 // every chain still flagged SEG_REPROJ, d = S^T z, dx += d (double-float),
 // r <- r - S d.
 template <int CPB>
-__global__ void __launch_bounds__(kPassThreads) defer_pass_kernel(const PassArgs a) {
+__global__ void __launch_bounds__(kPassThreads, 2) defer_pass_kernel(const PassArgs a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ float red[kPassWarps];
     __shared__ int live[CPB];
@@ -459,9 +461,11 @@ __global__ void __launch_bounds__(kPassThreads) defer_pass_kernel(const PassArgs
                 float hh[kSlots];
                 load_slots<false>(a.cols, base, len, t0, lane, ii, hh, nullptr);
 #pragma unroll
-                for (int u = 0; u < kSlots; ++u)
+                for (int u = 0; u < kSlots; ++u) {
+                    if (t0 + u >= len) break;
 #pragma unroll
                     for (int c = 0; c < CPB; ++c) d[c] = fmaf(hh[u], sm[c * per + ii[u]], d[c]);
+                }
             }
             if (j >= 0) {
 #pragma unroll
@@ -514,9 +518,11 @@ __global__ void __launch_bounds__(kPassThreads) defer_pass_kernel(const PassArgs
                 float hh[kSlots];
                 load_slots<false>(a.rows, base, len, t0, lane, ii, hh, nullptr);
 #pragma unroll
-                for (int u = 0; u < kSlots; ++u)
+                for (int u = 0; u < kSlots; ++u) {
+                    if (t0 + u >= len) break;
 #pragma unroll
                     for (int c = 0; c < CPB; ++c) acc[c] = fmaf(hh[u], sm[c * per + a.ldz + ii[u]], acc[c]);
+                }
             }
             if (i >= 0) {
 #pragma unroll
