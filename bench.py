@@ -115,12 +115,14 @@ def load_peaks():
     return 6800.0, "fallback"
 
 
-def profile_traffic_per_chain_step(workload):
-    """DRAM bytes per chain-step from the committed ncu summary of the chain kernel."""
+def profile_traffic_per_chain_step(workload, segmented=False):
+    """DRAM bytes per chain-step from the committed ncu summary of the chain kernel (the segmented
+    instantiation's figure when the run reprojected through the batched passes)."""
     p = ROOT / "profiles" / f"chain_kernel_{workload}.md"
     if not p.exists():
         return None
-    m = re.search(r"dram_bytes_per_chain_step:\s*([0-9.eE+-]+)", p.read_text())
+    key = "dram_bytes_per_chain_step_segmented" if segmented else "dram_bytes_per_chain_step"
+    m = re.search(key + r":\s*([0-9.eE+-]+)", p.read_text())
     return float(m.group(1)) if m else None
 
 
@@ -402,7 +404,7 @@ def run_gpu(args):
     chain_ms = sum(s["chain_ms"] for s in timed) / len(timed)
     launches = max(1, int(round(sum(max(1, s["segments"]) for s in timed) / len(timed))))
     achieved = alg_bytes / (chain_ms * 1e-3) / 1e9
-    tpcs = profile_traffic_per_chain_step(args.workload)
+    tpcs = profile_traffic_per_chain_step(args.workload, segmented=any(s["segments"] > 0 for s in timed))
     roofline = {"bound": "hbm", "kernel": "achr_chain_kernel", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": (tpcs * chain_steps) if tpcs is not None else None,
                 "peak_source": f"{peak_kind} hbm_gbs (burst copy)", "algorithmic_bytes_per_step": alg_bytes,
