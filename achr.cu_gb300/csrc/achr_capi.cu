@@ -1158,17 +1158,27 @@ achr_status achr_sample_batch(achr_ctx *const *ctxs, int32_t n_models, const int
         bs.max_residual = std::max(bs.max_residual, st.max_residual);
         bs.max_bound_violation = std::max(bs.max_bound_violation, st.max_bound_violation);
     }
-    // Idle time of the resident CTA slots at the end: the CTAs' exit times
-    // (when each found its queue empty) against the last one.
-    double cmax = 0.0, cmean = 0.0;
-    for (size_t c = 0; c < n_ctas; ++c) {
-        const double t = (double)(ts[(size_t)n_models + 1 + c] - ts[(size_t)n_models]) * 1e-6;
-        cmax = std::max(cmax, t);
-        cmean += t;
+    // Idle share of each queue's CTA slots at its end: (max - mean) / max of
+    // the exit times of its CTAs (when each found the queue empty), averaged
+    // over the queues weighted by their predicted work.
+    double imb = 0.0, wsum = 0.0;
+    size_t c0 = (size_t)n_models + 1;
+    for (const Group &G : groups) {
+        double cmax = 0.0, cmean = 0.0;
+        for (int c = 0; c < G.grid; ++c) {
+            const double t = (double)(ts[c0 + (size_t)c] - ts[(size_t)n_models]) * 1e-6;
+            cmax = std::max(cmax, t);
+            cmean += t;
+        }
+        c0 += (size_t)G.grid;
+        if (G.grid > 0 && cmax > 0.0) {
+            cmean /= (double)G.grid;
+            imb += G.work * (cmax - cmean) / cmax;
+            wsum += G.work;
+        }
     }
-    if (n_ctas) cmean /= (double)n_ctas;
     bs.graph_ms = total_ms;
-    bs.load_imbalance = cmax > 0 ? (cmax - cmean) / cmax : 0.0;
+    bs.load_imbalance = wsum > 0.0 ? imb / wsum : 0.0;
     if (stats) *stats = bs;
     return ACHR_OK;
 }

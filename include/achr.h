@@ -375,8 +375,9 @@ achr_status achr_autotune(achr_ctx *ctx, int32_t *threads_per_chain_out);
 
 typedef struct {
     double graph_ms;            /* device time of the whole batched launch */
-    double load_imbalance;      /* (max - mean) / max over the CTAs' exit times (from the launch):
-                                   the share of the resident CTA slots left idle at the end */
+    double load_imbalance;      /* per work queue, (max - mean) / max of its CTAs' exit times (the
+                                   share of its CTA slots left idle at its end), averaged over the
+                                   queues weighted by their predicted work */
     int64_t accepted, rejected, reprojections, stuck_chains;
     double max_residual, max_bound_violation;
 } achr_batch_stats;
