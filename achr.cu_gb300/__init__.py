@@ -162,6 +162,11 @@ _SIGNATURES = {
     "achr_sample_batch": (C.c_int, [C.POINTER(C.c_void_p), C.c_int32, C.POINTER(C.c_int32), C.c_int32, C.c_uint64,
                                     C.POINTER(C.c_void_p), C.POINTER(C.c_int64), C.c_void_p, C.POINTER(BatchStats),
                                     C.POINTER(C.c_double)]),
+    "achr_set_batch_tiles": (C.c_int, [C.c_int32]),
+    "achr_get_batch_tiles": (C.c_int32, []),
+    "achr_autotune_batch": (C.c_int, [C.POINTER(C.c_void_p), C.c_int32, C.POINTER(C.c_int32), C.c_int32, C.c_uint64,
+                                      C.POINTER(C.c_void_p), C.POINTER(C.c_int64), C.c_void_p,
+                                      C.POINTER(C.c_int32)]),
     "achr_sample_noalloc": (C.c_int, [C.POINTER(DeviceModel), C.POINTER(Options), C.c_uint64, C.c_uint64, C.c_int32,
                                       C.c_int32, C.c_void_p, C.c_int64, C.c_void_p, C.POINTER(Stats)]),
     "achr_set_directions": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_int32]),
@@ -508,6 +513,28 @@ def sample_batch(samplers, n_points, n_steps: int, d_outs, ld_outs, stream: int 
     st = BatchStats()
     _check(lib().achr_sample_batch(ctxs, k, pts, n_steps, seed, outs, lds, C.c_void_p(stream), C.byref(st), ms))
     return st.as_dict(), list(ms)
+
+
+def set_batch_tiles(tiles: int) -> None:
+    """Tile size of the batched work queues (achr_set_batch_tiles): an item holds the work queued
+    behind it divided by tiles x the queue's CTAs."""
+    _check(lib().achr_set_batch_tiles(tiles))
+
+
+def batch_tiles() -> int:
+    return int(lib().achr_get_batch_tiles())
+
+
+def autotune_batch(samplers, n_points, n_steps: int, d_outs, ld_outs, stream: int = 0, seed: int = 0) -> int:
+    """Time a short batched run with each tile setting (achr_autotune_batch) and keep the fastest."""
+    k = len(samplers)
+    ctxs = (C.c_void_p * k)(*[s._ctx for s in samplers])
+    pts = (C.c_int32 * k)(*n_points)
+    outs = (C.c_void_p * k)(*d_outs)
+    lds = (C.c_int64 * k)(*ld_outs)
+    best = C.c_int32()
+    _check(lib().achr_autotune_batch(ctxs, k, pts, n_steps, seed, outs, lds, C.c_void_p(stream), C.byref(best)))
+    return best.value
 
 
 def gemm_bf16(M: int, N: int, K: int, A0: int, B0: int, C_out: int, lda: int, ldb: int, ldc: int,

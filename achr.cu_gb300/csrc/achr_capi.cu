@@ -7,6 +7,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <atomic>
 #include <map>
 #include <mutex>
 #include <cstdio>
@@ -894,6 +895,10 @@ namespace {
 // Autotuning results per (default padded length, device): threads per chain.
 std::mutex g_tune_mutex;
 std::map<std::pair<int, int>, int> g_tune_cache;
+// Guided self-scheduling of the batched work queues: an item holds the work
+// queued behind it divided by (this x the queue's CTAs); set by
+// achr_set_batch_tiles or achr_autotune_batch.
+std::atomic<int> g_batch_tiles{4};
 
 struct StreamSet {
     std::vector<cudaStream_t> streams;
@@ -987,10 +992,11 @@ achr_status achr_sample_batch(achr_ctx *const *ctxs, int32_t n_models, const int
                                                   : (double)n_steps * (double)(bd * ept) * 1e-9;
     }
     // One work queue per configuration.  Items run longest model first; each
-    // item's tile of chains is sized (guided self-scheduling) to about a
-    // quarter of the work still queued behind it divided by the CTAs, so
-    // early items are large (few queue operations) and the last ones are
+    // item's tile of chains is sized (guided self-scheduling) to the work
+    // still queued behind it divided by `tiles` x the CTAs (4 unless tuned),
+    // so early items are large (few queue operations) and the last ones are
     // single chains (the launch ends evenly).
+    const int tiles = g_batch_tiles.load();
     struct Group {
         int bd, ept, grid = 0;
         std::vector<int> models;
@@ -1042,7 +1048,7 @@ achr_status achr_sample_batch(achr_ctx *const *ctxs, int32_t n_models, const int
         for (int k : G.models) {
             const double t = chain_time[(size_t)k];
             for (int p = 0; p < n_points[k];) {
-                long long tile = (long long)(left / (4.0 * G.grid * std::max(t, 1e-30)));
+                long long tile = (long long)(left / ((double)tiles * G.grid * std::max(t, 1e-30)));
                 tile = std::max(1LL, std::min(tile, (long long)(n_points[k] - p)));
                 G.items.push_back(make_int4(k, p, p + (int)tile, 0));
                 p += (int)tile;
@@ -1180,6 +1186,40 @@ achr_status achr_sample_batch(achr_ctx *const *ctxs, int32_t n_models, const int
     bs.graph_ms = total_ms;
     bs.load_imbalance = wsum > 0.0 ? imb / wsum : 0.0;
     if (stats) *stats = bs;
+    return ACHR_OK;
+}
+
+achr_status achr_set_batch_tiles(int32_t tiles) {
+    if (tiles < 1 || tiles > 1024) return fail(ACHR_ERR_INVALID, "tiles must be in [1, 1024]");
+    g_batch_tiles.store(tiles);
+    return ACHR_OK;
+}
+
+int32_t achr_get_batch_tiles(void) { return g_batch_tiles.load(); }
+
+achr_status achr_autotune_batch(achr_ctx *const *ctxs, int32_t n_models, const int32_t *n_points, int32_t n_steps,
+                                uint64_t seed, double *const *d_points_out, const int64_t *ld_out, void *stream,
+                                int32_t *tiles_out) {
+    static const int kCand[] = {1, 2, 4, 8, 16};
+    const int saved = g_batch_tiles.load();
+    int best = saved;
+    double best_ms = 1e300;
+    for (int c : kCand) {
+        g_batch_tiles.store(c);
+        achr_batch_stats st;
+        achr_status r = achr_sample_batch(ctxs, n_models, n_points, n_steps, seed, d_points_out, ld_out, stream, &st,
+                                          nullptr);
+        if (r != ACHR_OK) {
+            g_batch_tiles.store(saved);
+            return r;
+        }
+        if (st.graph_ms < best_ms) {
+            best_ms = st.graph_ms;
+            best = c;
+        }
+    }
+    g_batch_tiles.store(best);
+    if (tiles_out) *tiles_out = best;
     return ACHR_OK;
 }
 

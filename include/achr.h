@@ -402,6 +402,19 @@ achr_status achr_sample_batch(achr_ctx *const *ctxs, int32_t n_models, const int
                               uint64_t seed, double *const *d_points_out, const int64_t *ld_out, void *stream,
                               achr_batch_stats *stats, double *model_ms_out);
 
+/* Tile size of the batched work queues: each item holds the work still queued
+ * behind it divided by tiles x the queue's CTAs (default 4; 1..1024).  The
+ * setting is process-wide. */
+achr_status achr_set_batch_tiles(int32_t tiles);
+int32_t achr_get_batch_tiles(void);
+
+/* Time achr_sample_batch for n_steps (a short probe, into the caller's output
+ * buffers, which it overwrites) with tiles = 1, 2, 4, 8 and 16, keep the
+ * fastest as the process-wide setting and write it to tiles_out if non-NULL. */
+achr_status achr_autotune_batch(achr_ctx *const *ctxs, int32_t n_models, const int32_t *n_points, int32_t n_steps,
+                                uint64_t seed, double *const *d_points_out, const int64_t *ld_out, void *stream,
+                                int32_t *tiles_out);
+
 /* ---- Sampling without any allocation ---- */
 
 /* Largest model (reactions) achr_sample_noalloc accepts: its working data sits

@@ -119,3 +119,35 @@ def test_batch_work_queue_many_tiles(pkg, queue_models):
         off += p
     for s in samplers:
         s.close()
+
+
+def test_batch_tiles_do_not_change_the_points(pkg, queue_models):
+    """The tile setting changes only how the queue cuts the chains: points stay bitwise equal; the
+    batch autotuner keeps one of its candidates."""
+    torch = pytest.importorskip("torch")
+    samplers = []
+    for m, w, N in queue_models[:3]:
+        s = pkg.Sampler(m, w)
+        s.set_null_space(N)
+        samplers.append(s)
+    P = [900, 333, 77]
+    stream = torch.cuda.current_stream().cuda_stream
+    outs = [torch.zeros((s.n, p), dtype=torch.float64, device="cuda") for s, p in zip(samplers, P)]
+    ptrs = [o.data_ptr() for o in outs]
+    saved = pkg.batch_tiles()
+    try:
+        got = []
+        for tiles in (1, 16):
+            pkg.set_batch_tiles(tiles)
+            pkg.sample_batch(samplers, P, 17, ptrs, P, stream=stream, seed=31)
+            got.append([o.cpu().numpy() for o in outs])
+        for a, b in zip(*got):
+            assert np.array_equal(a, b)
+        best = pkg.autotune_batch(samplers, P, 5, ptrs, P, stream=stream, seed=1)
+        assert best in (1, 2, 4, 8, 16) and pkg.batch_tiles() == best
+        with pytest.raises(pkg.AchrError):
+            pkg.set_batch_tiles(0)
+    finally:
+        pkg.set_batch_tiles(saved)
+        for s in samplers:
+            s.close()
