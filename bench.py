@@ -802,7 +802,8 @@ def learned_study(pkg, diag, smp, warm, *, seed, train, rank, iters, lr, batch, 
                      "chain_steps_per_s": steps / (ms * 1e-3), "frozen_fluxes": summ["frozen_params"]}
     smp.set_directions(None)
     lp, ll = out["plain"], out["learned"]
-    fallback = ll["max_rhat"] >= 1.01 and lp["max_rhat"] < 1.01
+    # plain ACHR is the fallback: the learned sampler's figure stands only where it passes R-hat
+    fallback = ll["max_rhat"] >= 1.01
     return {
         **out,
         "learned_over_plain": ll["min_ess_per_s"] / lp["min_ess_per_s"],
