@@ -202,18 +202,28 @@ __device__ __forceinline__ void pass_verdict(const PassArgs &a, int p, float mx,
     }
 }
 
-__device__ __forceinline__ float block_max(float v, float *red) {
+// Per-warp maxima of NV values into red[i][warp] (lane 0 writes); the caller
+// synchronises once and one thread reduces over the warps, so a CTA reduces
+// every chain's values behind a single barrier.
+template <int NV>
+__device__ __forceinline__ void warp_max_to(float (&v)[NV], float (*red)[kPassWarps]) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
-    for (int o = 16; o; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
-    if (lane == 0) red[warp] = v;
-    __syncthreads();
-    float m = red[0];
+    for (int i = 0; i < NV; ++i) {
+        float x = v[i];
 #pragma unroll
-    for (int w = 1; w < kPassWarps; ++w) m = fmaxf(m, red[w]);
-    __syncthreads();
+        for (int o = 16; o; o >>= 1) x = fmaxf(x, __shfl_xor_sync(0xffffffffu, x, o));
+        if (lane == 0) red[i][warp] = x;
+    }
+}
+
+__device__ __forceinline__ float over_warps(const float *r) {
+    float m = r[0];
+#pragma unroll
+    for (int w = 1; w < kPassWarps; ++w) m = fmaxf(m, r[w]);
     return m;
 }
+
 
 // Shared-memory floats per chain of the pass kernels (multiples of 4, so every
 // chain's block starts on a 16-byte boundary): z (ldz floats) and d, as a
@@ -282,7 +292,7 @@ __device__ __forceinline__ void load_slots(const EllView &E, int base, int len, 
 template <int CPB, bool EXACT32>
 __global__ void __launch_bounds__(kPassThreads) defer_pass1_kernel(const PassArgs a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    __shared__ float red[kPassWarps];
+    __shared__ float redm[2 * CPB][kPassWarps];
     __shared__ int live[CPB];
     const size_t per = pass1_floats(a.ldz, a.ld);
     float *const sm = reinterpret_cast<float *>(smem_raw);
@@ -409,11 +419,21 @@ __global__ void __launch_bounds__(kPassThreads) defer_pass1_kernel(const PassArg
                 }
             }
         }
+        {
+            float v[2 * CPB];
 #pragma unroll
-        for (int c = 0; c < CPB; ++c) {
-            const float vmx = block_max(mx[c], red);
-            const float vm0 = block_max(m0[c], red);
-            if (tid == 0 && live[c]) {
+            for (int c = 0; c < CPB; ++c) {
+                v[c] = mx[c];
+                v[CPB + c] = m0[c];
+            }
+            warp_max_to<2 * CPB>(v, redm);
+        }
+        __syncthreads();
+        if (tid == 0) {
+#pragma unroll
+            for (int c = 0; c < CPB; ++c) {
+                if (!live[c]) continue;
+                const float vmx = over_warps(redm[c]), vm0 = over_warps(redm[CPB + c]);
                 const int p = p0 + c;
                 a.flags[p] |= SEG_CORR;  // dx holds a correction for the next launch
                 a.r0[p] = vm0;
@@ -430,7 +450,7 @@ __global__ void __launch_bounds__(kPassThreads) defer_pass1_kernel(const PassArg
 template <int CPB>
 __global__ void __launch_bounds__(kPassThreads, 2) defer_pass_kernel(const PassArgs a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    __shared__ float red[kPassWarps];
+    __shared__ float redm[CPB][kPassWarps];
     __shared__ int live[CPB];
     const size_t per = pass_floats(a.ldz, a.ld);
     float *const sm = reinterpret_cast<float *>(smem_raw);
@@ -538,10 +558,12 @@ __global__ void __launch_bounds__(kPassThreads, 2) defer_pass_kernel(const PassA
                 }
             }
         }
+        warp_max_to<CPB>(mx, redm);
+        __syncthreads();
+        if (tid == 0) {
 #pragma unroll
-        for (int c = 0; c < CPB; ++c) {
-            const float vmx = block_max(mx[c], red);
-            if (tid == 0 && live[c]) pass_verdict(a, p0 + c, vmx, a.r0[p0 + c]);
+            for (int c = 0; c < CPB; ++c)
+                if (live[c]) pass_verdict(a, p0 + c, over_warps(redm[c]), a.r0[p0 + c]);
         }
         __syncthreads();
     }
