@@ -154,6 +154,7 @@ struct GemmParams {
     float *C;
     long long ldc;
     int vec;  // 1: rows of C are 16-byte aligned (float4 stores)
+    int n_fast;  // tile order: 1 = N fastest (A, the larger operand, streamed once), 0 = M fastest
     unsigned long long *err;
     const unsigned long long *gate;  // non-NULL: skip the whole GEMM when *gate <= gate_max
     unsigned long long gate_max;
@@ -164,7 +165,10 @@ __device__ __forceinline__ void bar_arrive(unsigned bar) {
 }
 
 // Persistent: one CTA per SM walks the output tiles tile = blockIdx.x + k *
-// gridDim.x (M fastest, so CTAs working at the same time share B tiles in L2).
+// gridDim.x, along the dimension of the smaller operand fastest: the CTAs
+// working at the same time then share the tiles of the larger operand, which
+// leaves DRAM once, while the smaller one stays in L2 (with M fastest and
+// 100,000 rows of A, A would be read again for every 256 columns of B).
 // Two 256-column accumulators in tensor memory let the epilogue of one tile
 // overlap the MMAs of the next; the k-block ring runs on across tiles.
 __global__ void __launch_bounds__(kThreads, 1)
@@ -184,8 +188,8 @@ __global__ void __launch_bounds__(kThreads, 1)
     const unsigned *tmem_slot_ptr = reinterpret_cast<const unsigned *>(smem_raw + (tmem_slot - raw));
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int m_tiles = (p.M + kBM - 1) / kBM;
-    const int tiles = m_tiles * ((p.N + kBN - 1) / kBN);
+    const int m_tiles = (p.M + kBM - 1) / kBM, n_tiles = (p.N + kBN - 1) / kBN;
+    const int tiles = m_tiles * n_tiles;
     const int kb_split = p.K / kBK;
     const int total = kb_split * p.nsplit;
 
@@ -217,7 +221,8 @@ __global__ void __launch_bounds__(kThreads, 1)
         if (lane == 0) {
             int it = 0;  // k-blocks issued by this CTA so far (the ring position)
             for (int tile = blockIdx.x; tile < tiles && ok; tile += gridDim.x) {
-                const int m0 = (tile % m_tiles) * kBM, n0 = (tile / m_tiles) * kBN;
+                const int m0 = (p.n_fast ? tile / n_tiles : tile % m_tiles) * kBM;
+                const int n0 = (p.n_fast ? tile % n_tiles : tile / m_tiles) * kBN;
                 for (int kb = 0; kb < total; ++kb, ++it) {
                     const int s = it % kStages;
                     const unsigned round = (unsigned)(it / kStages);
@@ -294,7 +299,8 @@ __global__ void __launch_bounds__(kThreads, 1)
                 break;
             }
             tc_fence_after();
-            const int m0 = (tile % m_tiles) * kBM, n0 = (tile / m_tiles) * kBN;
+            const int m0 = (p.n_fast ? tile / n_tiles : tile % m_tiles) * kBM;
+            const int n0 = (p.n_fast ? tile % n_tiles : tile / m_tiles) * kBN;
             const int row = m0 + q * 32 + lane;
             float *crow = p.C + (long long)row * p.ldc;
             const unsigned acc = tmem + (unsigned)(b * (int)kBN) + ((unsigned)(q * 32) << 16);
@@ -394,6 +400,7 @@ cudaError_t launch_tc_gemm(const TcGemm &g, unsigned long long *err, cudaStream_
     p.C = g.C;
     p.ldc = g.ldc;
     p.vec = (((uintptr_t)g.C & 15u) == 0 && (g.ldc % 4) == 0) ? 1 : 0;
+    p.n_fast = g.M > g.N ? 1 : 0;
     p.err = err;
     p.gate = g.gate;
     p.gate_max = g.gate_max;
