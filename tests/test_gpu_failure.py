@@ -37,3 +37,27 @@ def test_generous_wait_limit_changes_nothing(pkg, small_model, golden):
         s.set_null_space(golden["N"])
         b, _ = s.sample(16, 15, seed=2)
     assert np.array_equal(a, b)
+
+
+def test_batched_queue_reports_timeout_and_device_stays_usable(pkg, small_model, golden):
+    """A model whose column waits run out inside the persistent work-queue launch: every CTA that
+    takes one of its items records the timeout and leaves the queue, the launch ends, the batch
+    call returns ACHR_ERR_TIMEOUT, and the next batch on the same device samples normally."""
+    torch = pytest.importorskip("torch")
+    bad = pkg.Sampler(small_model, golden["warmup"], wait_limit_ns=-1_000_000)
+    good = pkg.Sampler(small_model, golden["warmup"])
+    try:
+        for s in (bad, good):
+            s.set_null_space(golden["N"])
+        P = [40, 40]
+        outs = [torch.zeros((small_model.n_rxns, p), dtype=torch.float64, device="cuda") for p in P]
+        stream = torch.cuda.current_stream().cuda_stream
+        with pytest.raises(pkg.AchrError) as err:
+            pkg.sample_batch([good, bad], P, 12, [o.data_ptr() for o in outs], P, stream=stream, seed=4)
+        assert err.value.status == TIMEOUT
+        st, _ = pkg.sample_batch([good], [40], 12, [outs[0].data_ptr()], [40], stream=stream, seed=4)
+        ref, _ = good.sample(40, 12, seed=4)
+        assert st["accepted"] == 40 * 12 and np.array_equal(outs[0].cpu().numpy(), ref)
+    finally:
+        bad.close()
+        good.close()
