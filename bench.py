@@ -60,7 +60,9 @@ def parse_args():
                          "snapshots STEPS steps apart")
     ap.add_argument("--gemm", type=int, metavar="CHAINS", help="time the tensor-core GEMM alone at this N")
     ap.add_argument("--null-report", action="store_true", help="null-space set-up time and basis quality")
-    ap.add_argument("--cli", action="store_true", help="wall time of the drop-in CLI on the 72 x 95 fixture")
+    ap.add_argument("--cli", action="store_true",
+                    help="wall time of the drop-in CLI on the 72 x 95 fixture; with --chains P, at genome scale "
+                         "(the bench model as MPS and %%f CSV, P points x 2000 steps)")
     ap.add_argument("--learned", type=int, nargs=4, metavar=("CHAINS", "BURNIN", "SEGMENTS", "STEPS"),
                     help="learned-preconditioned hit-and-run against plain ACHR on this ESS schedule")
     ap.add_argument("--train-chains", type=int, default=65536)
@@ -1065,6 +1067,52 @@ def run_gemm(args):
     return 0
 
 
+def run_cli_genome(args):
+    """The drop-in command line at genome scale, as a user runs it: the 2766 x 3742 model written
+    as fixed MPS, its 7484 warmup points as the reference's %f CSV (the bench's own inputs),
+    `ACHRCuda model.mps warmup.csv 1 P 2000` with P = 100,000 (--chains to change), writing the
+    3.7 GB File0.  Wall-clock seconds of the whole process and the CLI's own phase lines."""
+    import importlib
+    import tempfile
+
+    import __graft_entry__ as ge
+
+    pkg = ge.load_package()
+    pkg.lib()
+    synth = importlib.import_module("achr_gb300.synthetic")
+    spec, model, S, warm, P, T = build_inputs("genome", pkg, synth, warmup_form="percent_f")
+    P = args.chains or P
+    row, col, val, lb, ub = synth.make_model(spec)
+    times, phases = [], []
+    with tempfile.TemporaryDirectory() as tmp:
+        mps, csv = Path(tmp) / "genome.mps", Path(tmp) / "genome_warmup.csv"
+        synth.write_mps(mps, spec.n_mets, spec.n_rxns, row, col, val, lb, ub, name="genome")
+        pkg.write_points_csv(csv, warm)
+        run_dir = Path(tmp) / "run"
+        run_dir.mkdir()
+        for k in range(args.warmup + args.steps):
+            t0 = time.perf_counter()
+            r = subprocess.run([str(pkg.cli_path()), str(mps), str(csv), "1", str(P), str(T), "--seed",
+                                str(args.seed + k)], cwd=run_dir, capture_output=True, text=True)
+            el = time.perf_counter() - t0
+            if r.returncode != 0:
+                raise SystemExit(f"ACHRCuda failed ({r.returncode}): {r.stderr[-400:]}")
+            if k >= args.warmup:
+                times.append(el)
+                phases.append({m.group(1): float(m.group(2)) for m in
+                               re.finditer(r"(Null space|Sampling) done in ([0-9.]+) seconds", r.stdout)})
+        size = (run_dir / "File0").stat().st_size
+        csv_bytes = csv.stat().st_size
+    wall = float(np.median(times))
+    line = {"metric": f"wall seconds (CLI, 1 file x {P} points x {T} steps)", "value": wall, "unit": "s",
+            "higher_is_better": False, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "dtype": "f64",
+            "data": "synthetic genome model; warmup CSV written with %f", "chain_steps_per_s": P * T / wall,
+            "file0_bytes": size, "warmup_csv_bytes": csv_bytes, "runs_s": times, "phases_s": phases,
+            "config": {"workload": f"genome CLI: ACHRCuda genome.mps genome_warmup.csv 1 {P} {T}"}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_cli(args):
     """The drop-in command line on the reference's smallest published configuration: a 72 x 95
     model (the committed fixture; the paper's E. coli core has the same size), 190 warmup points
@@ -1104,7 +1152,7 @@ def run_cli(args):
 def main():
     args = parse_args()
     if args.cli:
-        return run_cli(args)
+        return run_cli_genome(args) if args.workload == "genome" and args.chains else run_cli(args)
     if args.null_report:
         return run_null_report(args)
     if args.gemm:
