@@ -84,8 +84,9 @@ struct ChainArgs {
     // Segmented sampling (achr_defer.cu): the reference's per-chain reprojection
     // is deferred to a batched pass between launches.  A launch runs the steps
     // [step0, step0 + T) of every chain; a check step ends the chain's launch
-    // right after x <- x + t u: the kernel writes S x (as BF16 hi/lo, rows in
-    // the model's order) for a chain whose residual exceeds residual_tol, and
+    // right after x <- x + t u: the kernel writes S x (in FP64 and as BF16
+    // hi/lo, rows in the device order) for a chain whose residual exceeds
+    // residual_tol, and
     // the point and centre accumulator to chain-major state; the next launch
     // (after the batched reprojection has updated the points) clips the point
     // and adds it to the accumulator before its first step, as the reference
