@@ -922,13 +922,13 @@ def run_large(args):
     # Reprojection accuracy against the FP64 oracle on 64 chains: one more
     # segment without reprojection, snapshot, the snapshot moved off the null
     # space by a row-space vector of size 1e-6 (the residual a %f warmup leaves,
-    # well above the 1e-9 trigger, so the pass reprojects every one of them),
-    # then one reprojection pass.
+    # well above the 1e-9 trigger, so the passes reproject every one of them),
+    # then a reprojection of up to four passes.
     smp.sample_resume(P, Tr, period, True, x.data_ptr(), a.data_ptr(), P, stream=stream, seed=args.seed + 1)
     Xs = x[:, :64].cpu().numpy()
     Xs = Xs + S.T @ (1e-6 * np.random.default_rng(args.seed).standard_normal((S.shape[0], 64)))
     x[:, :64].copy_(torch.from_numpy(Xs))
-    r1 = smp.reproject(P, x.data_ptr(), P, d_centre_acc=a.data_ptr(), max_rounds=1, stream=stream)
+    r1 = smp.reproject(P, x.data_ptr(), P, d_centre_acc=a.data_ptr(), max_rounds=4, stream=stream)
     got = x[:, :64].cpu().numpy()
     ref = fp64_reprojection(S, model.lb, model.ub, Xs)
     moved = float(np.abs(ref - Xs).max())
