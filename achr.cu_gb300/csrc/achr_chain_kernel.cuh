@@ -538,10 +538,8 @@ __device__ __forceinline__ bool chain_run(const ChainArgs &a, int p_begin, int p
             for (int k = 0; k < EPT; ++k) {
                 const int i = tid + k * BD;
                 const bool real = i < a.n;
-                // (streaming loads and stores for the chain state: read once, written once
-                // per segment, they should not push the warmup matrix out of L2)
-                xs[i] = real ? __ldcs(a.seg_x + (size_t)p * (size_t)a.ld_seg + (size_t)i) : 0.0;
-                As[i] = real ? __ldcs(a.seg_A + (size_t)p * (size_t)a.ld_seg + (size_t)i) : 0.0;
+                xs[i] = real ? a.seg_x[(size_t)p * (size_t)a.ld_seg + (size_t)i] : 0.0;
+                As[i] = real ? a.seg_A[(size_t)p * (size_t)a.ld_seg + (size_t)i] : 0.0;
             }
         } else if (a.x_in) {  // resume: the chain's point and centre accumulator after step0 steps
 #pragma unroll
@@ -573,7 +571,7 @@ __device__ __forceinline__ bool chain_run(const ChainArgs &a, int p_begin, int p
                 const int i = tid + k * BD;
                 if (i < a.n) {
                     const size_t o = (size_t)p * (size_t)a.ld_seg + (size_t)i;
-                    xs[i] = (xs[i] - f32_to_f64_exact(__ldcs(a.seg_dxh + o))) - f32_to_f64_exact(__ldcs(a.seg_dxl + o));
+                    xs[i] = (xs[i] - f32_to_f64_exact(a.seg_dxh[o])) - f32_to_f64_exact(a.seg_dxl[o]);
                 }
             }
         }
@@ -1050,17 +1048,17 @@ __device__ __forceinline__ bool chain_run(const ChainArgs &a, int p_begin, int p
                             // integer operations, and the FP64 value is stored as it is)
                             unsigned short h, l;
                             split_bf16_bits(f64_to_f32_rz(rr[q]), h, l);
-                            __stcs(rh + q, h);  // device row order, as the batched passes read them
-                            __stcs(rl + q, l);
-                            __stcs(rd + q, rr[q]);
+                            rh[q] = h;  // device row order, as the batched passes read them
+                            rl[q] = l;
+                            rd[q] = rr[q];
                         }
                     }
 #pragma unroll
                     for (int k = 0; k < EPT; ++k) {
                         const int i = tid + k * BD;
                         if (i < a.n) {
-                            __stcs(a.seg_x + (size_t)p * (size_t)a.ld_seg + (size_t)i, xs[i]);
-                            __stcs(a.seg_A + (size_t)p * (size_t)a.ld_seg + (size_t)i, As[i]);
+                            a.seg_x[(size_t)p * (size_t)a.ld_seg + (size_t)i] = xs[i];
+                            a.seg_A[(size_t)p * (size_t)a.ld_seg + (size_t)i] = As[i];
                         }
                     }
                     if (tid == 0) {
@@ -1169,8 +1167,8 @@ __device__ __forceinline__ bool chain_run(const ChainArgs &a, int p_begin, int p
             for (int k = 0; k < EPT; ++k) {
                 const int i = tid + k * BD;
                 if (i < a.n) {
-                    __stcs(a.seg_x + (size_t)p * (size_t)a.ld_seg + (size_t)i, xs[i]);
-                    __stcs(a.seg_A + (size_t)p * (size_t)a.ld_seg + (size_t)i, As[i]);
+                    a.seg_x[(size_t)p * (size_t)a.ld_seg + (size_t)i] = xs[i];
+                    a.seg_A[(size_t)p * (size_t)a.ld_seg + (size_t)i] = As[i];
                 }
             }
             if (tid == 0)
