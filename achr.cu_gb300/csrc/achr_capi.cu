@@ -1024,7 +1024,7 @@ achr_status achr_sample_batch(achr_ctx *const *ctxs, int32_t n_models, const int
         size_t extra = 0;
         for (int k : G.models) {
             ChainArgs &a = args[(size_t)k];
-            if (a.pinv32 && a.m > G.bd * G.ept) a.pinv32 = nullptr;
+            if (a.pinv32 && a.m > a.ldw) a.pinv32 = nullptr;  // the residual stays below the column's padding
             if (a.pinv32) extra = std::max(extra, ((size_t)a.m * sizeof(float) + 15) & ~(size_t)15);
         }
         achr::ChainQueue probe{};

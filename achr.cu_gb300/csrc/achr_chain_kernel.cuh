@@ -476,6 +476,25 @@ __device__ __forceinline__ void chain_barriers(unsigned char *smem_raw, uint64_t
     never = reinterpret_cast<uint64_t *>(reinterpret_cast<int *>(bar + 1 + 8) + 2);
 }
 
+// Entries e = tid, tid + BD, ... < kTbl of the step table for steps s + e below
+// `end`: the step's Philox draw (uniform and warmup index) and 1 / (W + t).
+template <int BD>
+__device__ __forceinline__ void fill_step_table(const ChainArgs &a, StepEntry *tbl, unsigned long long chain, int s,
+                                                int end, int tid) {
+    for (int e = tid; e < kTbl; e += BD) {
+        const int st = s + e;
+        if (st < end) {
+            const Philox4 pd = step_draw(a.seed, chain, (uint32_t)st, 0u);
+            StepEntry en;
+            en.U = step_uniform(pd);
+            en.inv = 1.0 / (double)(a.W + st + a.centre_offset);
+            en.idx = warmup_index(pd, (uint32_t)a.W);
+            en.pad = 0;
+            tbl[e] = en;
+        }
+    }
+}
+
 // One CTA's share of a launch: chains p_begin, p_begin + p_step, ... below
 // p_end of the model `a` describes, then the CTA's statistics into
 // a.counters.  The staging barriers live in the shared-memory header; the
@@ -533,6 +552,28 @@ __device__ __forceinline__ bool chain_run(const ChainArgs &a, int p_begin, int p
 #define ACHR_CHAIN_ID (a.chain_offset + (unsigned long long)p)
         // Segmented sampling: the chain's state bits from the earlier launches.
         const unsigned sflags = SEG ? a.seg_flags[p] : 0u;
+        // The step table of the first kTbl steps and the first step's warmup column are
+        // requested before the chain's state is loaded, so that the copy's latency overlaps
+        // the state loads (and, in segmented launches, the correction and the check step's
+        // finish).  The column buffer is free: the previous chain ended with a barrier.
+        int tbase = a.step0 - kTbl;
+        int buf_col = -1;
+        bool inflight = false;
+        if (a.T > 0 && !(sflags & SEG_STUCK)) {
+            tbase = a.step0;
+            fill_step_table<BD>(a, tbl, ACHR_CHAIN_ID, a.step0, a.step0 + a.T, tid);
+            __syncthreads();
+            const int r0 = (int)tbl[0].idx;
+            if (r0 >= 0 && r0 < a.W) {  // (else the step loop records the failure)
+                if (tid == 0) {
+                    fence_proxy_async_smem();
+                    mbar_arrive_expect_tx(bar, column_bytes(a));
+                    tma_load_1d(ws, a.warmup + (size_t)r0 * (size_t)a.ldw, column_bytes(a), bar);
+                }
+                inflight = true;
+                buf_col = r0;
+            }
+        }
         if (sflags & SEG_STARTED) {
 #pragma unroll
             for (int k = 0; k < EPT; ++k) {
@@ -557,8 +598,7 @@ __device__ __forceinline__ bool chain_run(const ChainArgs &a, int p_begin, int p
                 As[i] = a.A0[i];
             }
         }
-        int buf_col = -1;
-        bool inflight = false, any_accepted = a.x_in != nullptr || (sflags & SEG_ACCEPTED), stuck = false;
+        bool any_accepted = a.x_in != nullptr || (sflags & SEG_ACCEPTED), stuck = false;
         bool seg_pending = false;  // this launch ended the chain after a check step's update
         const bool was_stuck = (sflags & SEG_STUCK) != 0;
         if (was_stuck) stuck = true;  // stopped in an earlier launch: no more steps
@@ -601,25 +641,13 @@ __device__ __forceinline__ bool chain_run(const ChainArgs &a, int p_begin, int p
         // The reference checks when the step count is a multiple of the period
         // (ACHRCuda.cu:325); a period of INT_MAX stands for "never".
         int chk = a.check_period == 0x7fffffff ? 1 : a.step0 % a.check_period;
-        int tbase = a.step0 - kTbl;
 
         for (int s = a.step0; s < (a.step0 + a.T) && !stuck && !failed && !seg_pending; ++s) {
             if (s - tbase >= kTbl) {
                 // refill the step table: entry e holds step tbase + e
                 tbase = s;
                 __syncthreads();
-                for (int e = tid; e < kTbl; e += BD) {
-                    const int st = s + e;
-                    if (st < (a.step0 + a.T)) {
-                        const Philox4 pd = step_draw(a.seed, ACHR_CHAIN_ID, (uint32_t)st, 0u);
-                        StepEntry en;
-                        en.U = step_uniform(pd);
-                        en.inv = 1.0 / (double)(a.W + st + a.centre_offset);
-                        en.idx = warmup_index(pd, (uint32_t)a.W);
-                        en.pad = 0;
-                        tbl[e] = en;
-                    }
-                }
+                fill_step_table<BD>(a, tbl, ACHR_CHAIN_ID, s, a.step0 + a.T, tid);
                 __syncthreads();
             }
             // this step's table entry (its fields are read where they are used)
@@ -1329,7 +1357,8 @@ cudaError_t launch_cfg_kernel(const ChainArgs &a_in, cudaStream_t stream, int ma
     // the residual in the staging buffer; it is used only when both fit
     // without costing a resident CTA per SM.
     const size_t zbytes = ((size_t)a.m * sizeof(float) + 15) & ~(size_t)15;
-    if (a.pinv32 && a.m > BD * EPT) a.pinv32 = nullptr;
+    // (its residual occupies the column buffer below the buffer's zero padding: m <= ldw)
+    if (a.pinv32 && a.m > a.ldw) a.pinv32 = nullptr;
     size_t smem = base + (a.pinv32 ? zbytes : 0);
     cudaError_t e = cudaFuncSetAttribute(KFN, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)std::max(smem, base));

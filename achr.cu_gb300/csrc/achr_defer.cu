@@ -752,7 +752,9 @@ bool defer_selected(const achr_ctx *ctx) {
     const achr_options &o = ctx->opt;
     if (o.check_period <= 0 || ctx->m <= 0) return false;
     const int np = chain_padded_length(ctx->n, o.threads_per_chain);
-    if (np == 0 || ctx->m > np) return false;  // S x is staged in the chain kernel's column buffer
+    // S x is staged in the chain kernel's column buffer, below its zero padding (the padding
+    // beyond the column's ldw entries must stay zero: padded reactions read it as their w)
+    if (np == 0 || ctx->m > ctx->ldw) return false;
     // Each BF16-split pass multiplies the remaining error by roughly 1.5e-6 times the
     // condition number of S S^T (measured: 1.9e-3 at 1265); beyond 2e4 the passes
     // converge too slowly to be worth it, and far beyond they diverge.
