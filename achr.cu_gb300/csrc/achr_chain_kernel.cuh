@@ -552,28 +552,6 @@ __device__ __forceinline__ bool chain_run(const ChainArgs &a, int p_begin, int p
 #define ACHR_CHAIN_ID (a.chain_offset + (unsigned long long)p)
         // Segmented sampling: the chain's state bits from the earlier launches.
         const unsigned sflags = SEG ? a.seg_flags[p] : 0u;
-        // The step table of the first kTbl steps and the first step's warmup column are
-        // requested before the chain's state is loaded, so that the copy's latency overlaps
-        // the state loads (and, in segmented launches, the correction and the check step's
-        // finish).  The column buffer is free: the previous chain ended with a barrier.
-        int tbase = a.step0 - kTbl;
-        int buf_col = -1;
-        bool inflight = false;
-        if (a.T > 0 && !(sflags & SEG_STUCK)) {
-            tbase = a.step0;
-            fill_step_table<BD>(a, tbl, ACHR_CHAIN_ID, a.step0, a.step0 + a.T, tid);
-            __syncthreads();
-            const int r0 = (int)tbl[0].idx;
-            if (r0 >= 0 && r0 < a.W) {  // (else the step loop records the failure)
-                if (tid == 0) {
-                    fence_proxy_async_smem();
-                    mbar_arrive_expect_tx(bar, column_bytes(a));
-                    tma_load_1d(ws, a.warmup + (size_t)r0 * (size_t)a.ldw, column_bytes(a), bar);
-                }
-                inflight = true;
-                buf_col = r0;
-            }
-        }
         if (sflags & SEG_STARTED) {
 #pragma unroll
             for (int k = 0; k < EPT; ++k) {
@@ -598,7 +576,8 @@ __device__ __forceinline__ bool chain_run(const ChainArgs &a, int p_begin, int p
                 As[i] = a.A0[i];
             }
         }
-        bool any_accepted = a.x_in != nullptr || (sflags & SEG_ACCEPTED), stuck = false;
+        int buf_col = -1;
+        bool inflight = false, any_accepted = a.x_in != nullptr || (sflags & SEG_ACCEPTED), stuck = false;
         bool seg_pending = false;  // this launch ended the chain after a check step's update
         const bool was_stuck = (sflags & SEG_STUCK) != 0;
         if (was_stuck) stuck = true;  // stopped in an earlier launch: no more steps
@@ -641,6 +620,7 @@ __device__ __forceinline__ bool chain_run(const ChainArgs &a, int p_begin, int p
         // The reference checks when the step count is a multiple of the period
         // (ACHRCuda.cu:325); a period of INT_MAX stands for "never".
         int chk = a.check_period == 0x7fffffff ? 1 : a.step0 % a.check_period;
+        int tbase = a.step0 - kTbl;
 
         for (int s = a.step0; s < (a.step0 + a.T) && !stuck && !failed && !seg_pending; ++s) {
             if (s - tbase >= kTbl) {
