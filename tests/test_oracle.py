@@ -125,3 +125,28 @@ def test_oracle_degenerate_direction_is_rejected(oracle_mod, pkg):
     pts, st = oracle_mod.sample(model, warm, N, 3, 2, 5, max_attempts=50)
     assert st["stuck_chains"] == 2 and st["accepted"] == 0 and st["rejected"] == 100
     assert np.all(pts == 0.0)
+
+
+def test_refined_null_space_is_orthogonal_to_rows_at_rounding_level(golden, small_model):
+    from cases import refined_null_space
+    from conftest import dense_S
+
+    S = dense_S(small_model)
+    N = refined_null_space(S, golden["N"])
+    assert N.shape == golden["N"].shape
+    assert np.abs(S @ N).max() < 1.5e-15 < np.abs(S @ golden["N"]).max()
+    assert np.abs(N.T @ N - np.eye(N.shape[1])).max() < 1e-14
+    # the same subspace, the columns keeping their direction
+    assert np.abs(N - golden["N"]).max() < 1e-13
+
+
+def test_golden_fixture_is_well_conditioned_for_parity(oracle_mod, golden, small_model):
+    """The %f fixture the deferred parity checks and smoke() use: a 1e-15 relative change of N moves
+    the oracle's points by far less than the 1e-10 bar (chord points rounded to six decimals, by
+    contrast, leave direction components near u_tol and move by ~1e-7)."""
+    rng = np.random.default_rng(0)
+    a, st = oracle_mod.sample(small_model, golden["warmup"], golden["N"], 7, 16, 30)
+    b, _ = oracle_mod.sample(small_model, golden["warmup"], golden["N"] * (1 + 1e-15 * rng.standard_normal(golden["N"].shape)),
+                             7, 16, 30)
+    assert st["reprojections"] > 0
+    assert np.abs(a - b).max() / max(1.0, np.abs(a).max()) < 1e-11
