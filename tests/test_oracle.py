@@ -129,7 +129,6 @@ def test_oracle_degenerate_direction_is_rejected(oracle_mod, pkg):
 
 def test_refined_null_space_is_orthogonal_to_rows_at_rounding_level(golden, small_model):
     from cases import refined_null_space
-    from conftest import dense_S
 
     S = dense_S(small_model)
     N = refined_null_space(S, golden["N"])
