@@ -1326,8 +1326,7 @@ __global__ void __launch_bounds__(BD, (BD <= 384 ? 2 : 1)) achr_chain_queue_kern
 }
 
 // Occupancy-sized persistent launch of one configuration.  max_ctas > 0 caps
-// the grid; max_ctas < 0 launches one CTA per chain, leaving the balancing of
-// concurrent launches to the hardware CTA scheduler (batched models).
+// the grid.
 template <int BD, int EPT, bool SEG>
 cudaError_t launch_cfg_kernel(const ChainArgs &a_in, cudaStream_t stream, int max_ctas, int *per_sm_out) {
     auto *const KFN = achr_chain_kernel<BD, EPT, SEG>;
@@ -1361,7 +1360,7 @@ cudaError_t launch_cfg_kernel(const ChainArgs &a_in, cudaStream_t stream, int ma
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    long long grid = max_ctas < 0 ? (long long)a.P : (long long)sms * per_sm;
+    long long grid = (long long)sms * per_sm;
     if (max_ctas > 0 && grid > max_ctas) grid = max_ctas;
     if (grid > a.P) grid = a.P;
     if (grid < 1) return cudaSuccess;
