@@ -50,6 +50,7 @@
 
 #include <algorithm>
 #include <cstring>
+#include <memory>
 #include <new>
 #include <string>
 #include <vector>
@@ -671,12 +672,10 @@ EllView view(const SlicedEll &E) {
     return EllView{E.groups, E.off.p, E.line.p, E.idx.p, E.vh.p, E.vl.p};
 }
 
-achr_status ensure_defer(achr_ctx *ctx, int chains, int segments) {
-    DeferState *D = ctx->defer;
-    if (!D) {
-        D = new (std::nothrow) DeferState();
-        if (!D) return set_err(ACHR_ERR_NOMEM, "allocation failed");
-        ctx->defer = D;
+// The per-model part of the state (B in the device row order, the sliced-ELL
+// blocks); the context takes it only once all of it is built.
+achr_status init_defer(const achr_ctx *ctx, DeferState *D) {
+    {
         const ReprojState &R = *ctx->reproj;
         D->kpad = R.kpad;
         D->ld = (ctx->n + 1) & ~1;
@@ -726,6 +725,18 @@ achr_status ensure_defer(achr_ctx *ctx, int chains, int segments) {
         st = build_ell(D->rows, m, rp, ci, rv, exact, false);  // line q is device row q
         if (st != ACHR_OK) return st;
         D->exact32 = exact;
+    }
+    return ACHR_OK;
+}
+
+achr_status ensure_defer(achr_ctx *ctx, int chains, int segments) {
+    DeferState *D = ctx->defer;
+    if (!D) {
+        std::unique_ptr<DeferState> nd(new (std::nothrow) DeferState());
+        if (!nd) return set_err(ACHR_ERR_NOMEM, "allocation failed");
+        const achr_status st = init_defer(ctx, nd.get());
+        if (st != ACHR_OK) return st;
+        D = ctx->defer = nd.release();
     }
     if (D->cap < chains) {
         D->cap = 0;
