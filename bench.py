@@ -440,6 +440,8 @@ def run_gpu(args):
             torch.cuda.synchronize()
             e2e_times.append(time.perf_counter() - t0)
         e2e_s = max(sum(e2e_times) / len(e2e_times), 1e-9)
+        if world > 1:  # the job's end-to-end time is the slowest rank's
+            e2e_s = sharding.max_over_ranks(e2e_s, device="cuda")
         h2d = warm.size * 8 + len(model.row) * 16 + n * 16
         e2e = {"value": world * chain_steps / e2e_s, "unit": METRIC, "h2d_bytes_per_step": int(h2d),
                "d2h_bytes_per_step": int(n * P * 8), "seconds_per_step": e2e_s}
