@@ -17,6 +17,7 @@
 
 #include "../../include/achr.h"
 #include "achr_ctx.h"
+#include "achr_queue_plan.h"
 
 using achr::ChainArgs;
 using achr::DevBuf;
@@ -991,11 +992,8 @@ achr_status achr_sample_batch(achr_ctx *const *ctxs, int32_t n_models, const int
         chain_time[(size_t)k] = c->tuned_rate > 0 ? (double)n_steps / c->tuned_rate
                                                   : (double)n_steps * (double)(bd * ept) * 1e-9;
     }
-    // One work queue per configuration.  Items run longest model first; each
-    // item's tile of chains is sized (guided self-scheduling) to the work
-    // still queued behind it divided by `tiles` x the CTAs (4 unless tuned),
-    // so early items are large (few queue operations) and the last ones are
-    // single chains (the launch ends evenly).
+    // One work queue per configuration, its items from plan_queue
+    // (achr_queue_plan.h) with `tiles` = 4 unless tuned.
     const int tiles = g_batch_tiles.load();
     struct Group {
         int bd, ept, grid = 0;
@@ -1042,19 +1040,8 @@ achr_status achr_sample_batch(achr_ctx *const *ctxs, int32_t n_models, const int
         }
         G.extra = extra;
         G.grid = sms * per_sm;
-        std::stable_sort(G.models.begin(), G.models.end(),
-                         [&](int x, int y) { return chain_time[(size_t)x] > chain_time[(size_t)y]; });
-        double left = G.work;
-        for (int k : G.models) {
-            const double t = chain_time[(size_t)k];
-            for (int p = 0; p < n_points[k];) {
-                long long tile = (long long)(left / ((double)tiles * G.grid * std::max(t, 1e-30)));
-                tile = std::max(1LL, std::min(tile, (long long)(n_points[k] - p)));
-                G.items.push_back(make_int4(k, p, p + (int)tile, 0));
-                p += (int)tile;
-                left -= (double)tile * t;
-            }
-        }
+        for (const achr::QueueItem &q : achr::plan_queue(G.models, n_points, chain_time.data(), G.grid, tiles))
+            G.items.push_back(make_int4(q.model, q.p0, q.p1, 0));
         total_items += G.items.size();
     }
     std::stable_sort(groups.begin(), groups.end(), [](const Group &x, const Group &y) { return x.work > y.work; });
